@@ -1,0 +1,331 @@
+"""Benchmark of the upwind advection hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--arith auto|fixed|fma|exact] [--no-cpu-baseline]
+
+Workload (one bench step): advect(100 steps, dt) of the 512^3 FP64 periodic
+unit cube, v = (1.0, -0.7, 0.3), dt = 0.5 min_j dx_j/|v_j| = 0.5/512, initial
+field = sphere indicator (centre 0.5^3, radius 0.2) + seeded uniform noise in
+[0, 0.01) (seed 20261203).  Metric: FP64 cell updates per second (GCUPS).
+
+  value        device-timed: K bench steps between CUDA events on the
+               library's stream, field resident in HBM (1 GiB per buffer, far
+               larger than L2, so no flush is needed between steps).
+  e2e          the same metric through the public API with host buffers:
+               every step uploads the initial field from pinned host memory,
+               advects, downloads the field and reads the checksum.
+  roofline     the step kernel's achieved bandwidth on the 16 B/cell-update
+               algorithmic basis (read f once, write f once) against the
+               measured HBM copy peak.
+  cpu_baseline the reference algorithm (oracle/_ref when it was compiled in
+               this tree, else the oracle's C restatement) on the host cores,
+               on a bounded sample of the same workload.
+
+`--impl reference` times that CPU implementation alone (the reference arm).
+Under torchrun (N > 1) every rank runs an independent replica ("replicas
+only": the plain form does not shard) and rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_AXIS = 512
+SHAPE = (N_AXIS, N_AXIS, N_AXIS)
+VELOCITY = (1.0, -0.7, 0.3)
+LENGTHS = (1.0, 1.0, 1.0)
+TIME_STEPS = 100
+DT = 0.5 / N_AXIS
+SEED = 20261203
+CENTER = (0.5, 0.5, 0.5)
+RADIUS = 0.2
+NOISE = 0.01
+BYTES_PER_CELL_UPDATE = 16.0  # read f, write f (FP64)
+WORKLOAD = "upwind3d_f64_512cube_100steps"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(kernel: str):
+    """DRAM bytes per cell-update of `kernel` from the committed ncu summary
+    (profiles/traffic_per_cell_update.txt: `<kernel> <bytes> <source>`)."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_cell_update.txt")
+    try:
+        for line in open(p):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the
+    timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        loaded = [s for s in sm if smax and s >= 0.3 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_sample(threads: int | None = None, time_steps: int = 2):
+    """Reference algorithm on the host: a bounded sample of the workload (the
+    full 512^3 field, `time_steps` time steps), all host threads."""
+    from oracle import Port, Reference
+    port = Port()
+    f0 = port.sphere_noise(SHAPE, LENGTHS, CENTER, RADIUS, NOISE, SEED)
+    threads = threads or os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    kind = "port"
+    impl = port
+    if Reference.available():
+        try:
+            impl = Reference()
+            kind = "reference"
+        except OSError:
+            impl = port
+    if kind == "reference":
+        _, el = impl.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, time_steps, DT)
+    else:
+        _, el = impl.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, time_steps, DT, threads=threads)
+    cells = float(np.prod(SHAPE)) * time_steps
+    return {"value": cells / el / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
+            "sample": f"512^3 x {time_steps} time steps (of the workload's 100), "
+                      f"{el:.2f} s, OMP_NUM_THREADS={threads}, "
+                      + ("reference upwind.cxx compiled by oracle/Makefile" if kind == "reference"
+                         else "oracle C restatement, -O3 -fopenmp -ffp-contract=off")}
+
+
+def run_reference_arm(args, ws, rank) -> None:
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(threads, time_steps=1)
+    vals = [cpu_sample(threads, time_steps=1) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    base = dict(vals[0])
+    base["value"] = v
+    base["sample"] = f"512^3 x 1 time step per bench step, median of {args.steps}; " + \
+        base["sample"].split(", ", 1)[1]
+    ms = float(np.prod(SHAPE)) * TIME_STEPS / (v * 1e9) * 1e3
+    print(json.dumps({
+        "impl": "reference", "metric": "FP64 GCUPS (upwind advection, 512^3 periodic)",
+        "value": v, "unit": "GCUPS", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "velocity": list(VELOCITY),
+                   "time_steps": TIME_STEPS, "dt": DT, "l2": "inputs larger than L2 (1 GiB field)"},
+        "cpu_baseline": base,
+        "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arith", default="auto", choices=["auto", "fixed", "fma", "exact"])
+    ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import fidibench_gb300 as fdb
+    from fidibench_gb300._capi import lib
+
+    up = fdb.Upwind(VELOCITY, LENGTHS, SHAPE, arith=args.arith, depth=args.depth)
+    stream = torch.cuda.Stream()
+    up.set_stream(stream)
+    up.init_sphere(CENTER, RADIUS, NOISE, SEED)
+    cells = float(np.prod(SHAPE))
+
+    for _ in range(args.warmup):
+        up.advect(TIME_STEPS, DT)
+    stream.synchronize()
+    arith_used = up.arith_used
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-timed region --------------------------------------------------
+    clocks = ClockSampler(local) if rank == 0 else None
+    barrier()
+    l0 = lib.fdb_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        up.advect(TIME_STEPS, DT)
+    e1.record(stream)
+    barrier()
+    launches = int(lib.fdb_launch_count() - l0)
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop() if clocks else None
+    t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = ws * cells * TIME_STEPS * args.steps / (ms_max * 1e-3) / 1e9
+
+    # ---- roofline of the step kernel --------------------------------------------
+    peak, peak_kind = load_peaks()
+    step_launches = max(launches, 1)
+    cell_updates_per_launch = cells * TIME_STEPS * args.steps / step_launches
+    avg_launch_s = ms_total * 1e-3 / step_launches
+    achieved = BYTES_PER_CELL_UPDATE * cell_updates_per_launch / avg_launch_s / 1e9
+    kernel_name = {"fixed": "k_advect_fixed", "fma": "k_step3_fma",
+                   "exact": "k_step3_exact"}.get(arith_used, arith_used)
+    tpc = load_traffic(kernel_name)
+
+    # ---- end to end through the public API with host buffers -----------------------
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty(int(cells), dtype=torch.float64, pin_memory=True)
+        host_out = torch.empty(int(cells), dtype=torch.float64, pin_memory=True)
+        up.get_field(host_in)  # a real field as input
+        for _ in range(2):
+            up.set_field(host_in)
+            up.advect(TIME_STEPS, DT)
+            up.get_field(host_out)
+            up.checksum()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            up.set_field(host_in)
+            up.advect(TIME_STEPS, DT)
+            up.get_field(host_out)
+            up.checksum()
+        barrier()
+        el = time.perf_counter() - t0
+        te = torch.tensor([el], device="cuda", dtype=torch.float64)
+        if dist is not None:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        el = float(te.item())
+        e2e = {"value": ws * cells * TIME_STEPS * args.steps / el / 1e9, "unit": "GCUPS",
+               "h2d_bytes_per_step": int(cells) * 8, "d2h_bytes_per_step": int(cells) * 8 + 8}
+    up.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample()
+
+    if rank == 0:
+        line = {
+            "metric": "FP64 GCUPS (upwind advection, 512^3 periodic)",
+            "value": value, "unit": "GCUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if arith_used != "fixed" else "f64 (i64 block-fixed-point arithmetic)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "shape": list(SHAPE), "velocity": list(VELOCITY),
+                       "time_steps": TIME_STEPS, "dt": DT, "arith": arith_used,
+                       "init": "sphere r=0.2 + U[0,0.01) noise, seed 20261203",
+                       "l2": "inputs larger than L2 (1 GiB field per buffer)",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None if tpc is None else tpc * cell_updates_per_launch,
+                         "kernel": kernel_name,
+                         "basis": "16 B algorithmic per cell-update"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""ctypes binding of libfdb_upwind.so (the C-ABI in include/fdb_upwind.h).
+
+The library is loaded from the package's in-tree ``_lib/`` directory.  There
+is no fallback: if the shared library is missing or was built for another
+host, importing this module raises, so no caller can silently end up on a CPU
+path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfdb_upwind.so")
+
+FDB_OK = 0
+FDB_ERR_INVALID = 1
+FDB_ERR_CUDA = 2
+FDB_ERR_ALLOC = 3
+FDB_ERR_UNSUPPORTED = 4
+FDB_ERR_TIMEOUT = 5
+FDB_ERR_NONFINITE = 6
+FDB_ERR_INJECTED = 7
+FDB_MAX_DIMS = 8
+
+ARITH_AUTO = 0
+ARITH_EXACT = 1
+ARITH_FMA = 2
+ARITH_FIXED = 3
+ARITH_NAMES = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fma": ARITH_FMA, "fixed": ARITH_FIXED}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_vp = ctypes.c_void_p
+_int = ctypes.c_int
+
+# name -> (restype, argtypes); every symbol declared in include/*.h
+SIGNATURES: dict[str, tuple] = {
+    "fdb_last_error": (ctypes.c_char_p, []),
+    "fdb_version": (ctypes.c_char_p, []),
+    "fdb_launch_count": (ctypes.c_uint64, []),
+    "fdb_upwind_create": (_int, [_int, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "fdb_upwind_destroy": (_int, [_vp]),
+    "fdb_upwind_set_field": (_int, [_vp, _vp, _int]),
+    "fdb_upwind_get_field": (_int, [_vp, _vp, _int]),
+    "fdb_upwind_field_ptr": (_int, [_vp, ctypes.POINTER(_vp)]),
+    "fdb_upwind_advect": (_int, [_vp, _int, ctypes.c_double]),
+    "fdb_upwind_checksum": (_int, [_vp, _dp]),
+    "fdb_upwind_std": (_int, [_vp, _dp]),
+    "fdb_upwind_set_stream": (_int, [_vp, _vp]),
+    "fdb_upwind_set_arith": (_int, [_vp, _int, _int]),
+    "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
+    "fdb_upwind_init_sphere": (_int, [_vp, _vp, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_uint64]),
+    "fdb_upwind_adjoint": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _vp, _int, _int]),
+    "fdb_upwind_adjoint_step": (_int, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
+}
+
+
+class FdbError(RuntimeError):
+    """A non-zero status from libfdb_upwind, with fdb_last_error()'s text."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fdb error {code}: {msg}")
+        self.code = code
+
+
+def _load() -> ctypes.CDLL:
+    if not os.path.isfile(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python fidibench_gb300/build.py` "
+            "(the CUDA library is required; there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def check(rc: int) -> None:
+    if rc != FDB_OK:
+        raise FdbError(rc, lib.fdb_last_error().decode(errors="replace"))
+
+
+def dptr(a) -> int | None:
+    """Address of a contiguous numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

@@ -1,0 +1,456 @@
+// capi.cu -- the C-ABI of libfdb_upwind (declared in include/fdb_upwind.h).
+//
+// One handle = one problem on the current CUDA device: two FP64 fields used
+// as a ping-pong pair (the reference keeps f plus an oldF copy and copies
+// every step, upwind/cxx/upwind.cxx:53-62; here the step reads one buffer and
+// writes the other), small reduction scratch, and lazily allocated adjoint
+// checkpoint storage.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "fdb_internal.h"
+
+struct fdb_upwind {
+  fdb::Geom g;
+  double* buf[2] = {nullptr, nullptr};
+  int cur = 0;
+  double* part = nullptr;     // reduction partials (reduce_partials(ntot))
+  double* dscal = nullptr;    // device scalars [8]
+  double* dpart = nullptr;    // adjoint per-CTA coefficient partials [3 * adjoint_blocks()]
+  double* hscal = nullptr;    // pinned host scalars [8]
+  double* scratch = nullptr;  // kernel scratch for the fixed-point path
+  size_t scratch_bytes = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int arith = FDB_ARITH_AUTO;
+  int depth = 0;
+  int arith_used = 0;
+  // adjoint storage
+  std::vector<double*> ckpt;
+  std::vector<double*> seg;
+  double* lam[2] = {nullptr, nullptr};
+};
+
+namespace fdb {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return FDB_ERR_CUDA;
+}
+
+static std::atomic<uint64_t> g_launches{0};
+
+void note_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+bool fault_injected(const char* kind) {
+  const char* f = getenv("FDB_FAULT");
+  return f && strcmp(f, kind) == 0;
+}
+
+int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g) {
+  if (ndims < 1 || ndims > FDB_MAX_DIMS) return fail(FDB_ERR_INVALID, "ndims must be in [1, 8]");
+  if (!v || !L || !n) return fail(FDB_ERR_INVALID, "null velocity/lengths/num_cells");
+  Geom r;
+  r.ndims = ndims;
+  r.ntot = 1;
+  for (int j = 0; j < ndims; ++j) {
+    if (n[j] == 0) return fail(FDB_ERR_INVALID, "num_cells must be positive on every axis");
+    if (!(L[j] > 0.0) || !isfinite(L[j])) return fail(FDB_ERR_INVALID, "lengths must be finite and > 0");
+    if (!isfinite(v[j])) return fail(FDB_ERR_INVALID, "velocity must be finite");
+    if (r.ntot > (UINT64_MAX / 16) / n[j]) return fail(FDB_ERR_INVALID, "grid too large");
+    r.n[j] = n[j];
+    r.v[j] = v[j];
+    r.L[j] = L[j];
+    // upwind.cxx:34-36
+    r.up[j] = (v[j] < 0.) ? +1 : -1;
+    r.dx[j] = L[j] / (double)n[j];
+    r.ntot *= n[j];
+  }
+  r.dimProd[ndims - 1] = 1;
+  for (int i = ndims - 2; i >= 0; --i) r.dimProd[i] = r.dimProd[i + 1] * r.n[i + 1];
+  if (ndims <= 3) {
+    const int pad = 3 - ndims;
+    int64_t nn[3] = {1, 1, 1};
+    int uu[3] = {-1, -1, -1};
+    int jj[3] = {-1, -1, -1};
+    for (int j = 0; j < ndims; ++j) {
+      nn[pad + j] = (int64_t)r.n[j];
+      uu[pad + j] = r.up[j];
+      jj[pad + j] = j;
+    }
+    r.nz = nn[0]; r.ny = nn[1]; r.nx = nn[2];
+    r.upz = uu[0]; r.upy = uu[1]; r.upx = uu[2];
+    r.jz = jj[0]; r.jy = jj[1]; r.jx = jj[2];
+  }
+  *g = r;
+  return FDB_OK;
+}
+
+double ref_coeff(const Geom& g, int j, double dt) {
+  // deltaTime * this->v[j] * this->upDirection[j] / this->deltas[j]
+  return dt * g.v[j] * (double)g.up[j] / g.dx[j];
+}
+
+Coeffs3 coeffs3(const Geom& g, double dt) {
+  Coeffs3 c{};
+  c.cz = g.jz >= 0 ? ref_coeff(g, g.jz, dt) : 0.0;
+  c.cy = g.jy >= 0 ? ref_coeff(g, g.jy, dt) : 0.0;
+  c.cx = g.jx >= 0 ? ref_coeff(g, g.jx, dt) : 0.0;
+  c.az = -c.cz;
+  c.ay = -c.cy;
+  c.ax = -c.cx;
+  c.w = ((1.0 - c.az) - c.ay) - c.ax;
+  return c;
+}
+
+}  // namespace fdb
+
+using namespace fdb;
+
+namespace {
+
+int check_handle(fdb_upwind* h) {
+  if (!h) return fail(FDB_ERR_INVALID, "null handle");
+  return FDB_OK;
+}
+
+int sync(fdb_upwind* h) {
+  FDB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return FDB_OK;
+}
+
+void free_adjoint(fdb_upwind* h) {
+  for (double* p : h->ckpt) cudaFree(p);
+  for (double* p : h->seg) cudaFree(p);
+  h->ckpt.clear();
+  h->seg.clear();
+  for (int k = 0; k < 2; ++k) {
+    if (h->lam[k]) cudaFree(h->lam[k]);
+    h->lam[k] = nullptr;
+  }
+}
+
+int dalloc(double** p, size_t count) {
+  if (fault_injected("alloc")) return fail(FDB_ERR_INJECTED, "injected allocation failure");
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(double));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(FDB_ERR_ALLOC, std::string("cudaMalloc of ") + std::to_string(count * 8) +
+                                   " bytes failed: " + cudaGetErrorString(e));
+  }
+  return FDB_OK;
+}
+
+int resolve_arith(fdb_upwind* h, const Coeffs3& c) {
+  const Geom& g = h->g;
+  if (g.ndims > 3) return FDB_ARITH_EXACT;  // generic kernel
+  if (h->arith == FDB_ARITH_EXACT || h->arith == FDB_ARITH_FMA) return h->arith;
+  const bool ok = fixed_supported(g, c, h->depth) == FDB_OK;
+  if (h->arith == FDB_ARITH_FIXED && !ok) return -1;
+  return ok ? FDB_ARITH_FIXED : FDB_ARITH_FMA;
+}
+
+// Advance the handle's field by `steps` steps with the given arithmetic.
+int advance(fdb_upwind* h, int steps, double dt, int arith) {
+  const Geom& g = h->g;
+  if (g.ndims > 3) {
+    for (int s = 0; s < steps; ++s) {
+      FDB_TRY(launch_step_generic(g, dt, h->buf[h->cur], h->buf[h->cur ^ 1], h->stream));
+      h->cur ^= 1;
+    }
+    return FDB_OK;
+  }
+  const Coeffs3 c = coeffs3(g, dt);
+  if (arith == FDB_ARITH_FIXED)
+    return launch_advect_fixed(g, c, steps, h->depth, h->buf, &h->cur, h->scratch,
+                               h->scratch_bytes, h->stream);
+  for (int s = 0; s < steps; ++s) {
+    FDB_TRY(launch_step_f64(g, c, arith, h->buf[h->cur], h->buf[h->cur ^ 1], h->stream));
+    h->cur ^= 1;
+  }
+  return FDB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fdb_last_error(void) { return g_err.c_str(); }
+
+const char* fdb_version(void) { return "fidibench_gb300 0.1.0 (sm_103a)"; }
+
+uint64_t fdb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
+                      const uint64_t* num_cells, fdb_upwind** out) {
+  if (!out) return fail(FDB_ERR_INVALID, "null output handle pointer");
+  *out = nullptr;
+  Geom g;
+  FDB_TRY(make_geom(ndims, velocity, lengths, num_cells, &g));
+  fdb_upwind* h = new fdb_upwind();
+  h->g = g;
+  int rc = FDB_OK;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    rc = cuda_fail(e, "cudaStreamCreate");
+    delete h;
+    return rc;
+  }
+  h->stream = h->own;
+  if ((rc = dalloc(&h->buf[0], g.ntot)) || (rc = dalloc(&h->buf[1], g.ntot)) ||
+      (rc = dalloc(&h->part, reduce_partials(g.ntot))) || (rc = dalloc(&h->dscal, 8)) ||
+      (rc = dalloc(&h->dpart, 3 * (size_t)adjoint_blocks()))) {
+    fdb_upwind_destroy(h);
+    return rc;
+  }
+  e = cudaMallocHost((void**)&h->hscal, 8 * sizeof(double));
+  if (e != cudaSuccess) {
+    fdb_upwind_destroy(h);
+    return cuda_fail(e, "cudaMallocHost");
+  }
+  // f = 0, f[0] = 1 (upwind.cxx:45-48)
+  rc = launch_fill_corner(h->buf[0], g.ntot, h->stream);
+  if (!rc) rc = sync(h);
+  if (rc) {
+    fdb_upwind_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return FDB_OK;
+}
+
+int fdb_upwind_destroy(fdb_upwind* h) {
+  if (!h) return FDB_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_adjoint(h);
+  for (int k = 0; k < 2; ++k)
+    if (h->buf[k]) cudaFree(h->buf[k]);
+  if (h->part) cudaFree(h->part);
+  if (h->dscal) cudaFree(h->dscal);
+  if (h->dpart) cudaFree(h->dpart);
+  if (h->scratch) cudaFree(h->scratch);
+  if (h->hscal) cudaFreeHost(h->hscal);
+  if (h->own) cudaStreamDestroy(h->own);
+  delete h;
+  return FDB_OK;
+}
+
+int fdb_upwind_set_field(fdb_upwind* h, const double* src, int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!src) return fail(FDB_ERR_INVALID, "null source field");
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->buf[h->cur], src, h->g.ntot * sizeof(double),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               h->stream));
+  return sync(h);
+}
+
+int fdb_upwind_get_field(fdb_upwind* h, double* dst, int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!dst) return fail(FDB_ERR_INVALID, "null destination field");
+  FDB_CUDA_TRY(cudaMemcpyAsync(dst, h->buf[h->cur], h->g.ntot * sizeof(double),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  return sync(h);
+}
+
+int fdb_upwind_field_ptr(fdb_upwind* h, double** out) {
+  FDB_TRY(check_handle(h));
+  if (!out) return fail(FDB_ERR_INVALID, "null output pointer");
+  *out = h->buf[h->cur];
+  return FDB_OK;
+}
+
+int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt) {
+  FDB_TRY(check_handle(h));
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
+  if (num_steps == 0) return FDB_OK;
+  int arith = FDB_ARITH_EXACT;
+  if (h->g.ndims <= 3) {
+    arith = resolve_arith(h, coeffs3(h->g, dt));
+    if (arith < 0)
+      return fail(FDB_ERR_UNSUPPORTED,
+                  "FDB_ARITH_FIXED requested but the geometry/coefficients are outside its "
+                  "domain (see fdb_upwind_set_arith)");
+  }
+  h->arith_used = arith;
+  return advance(h, num_steps, dt, arith);
+}
+
+int fdb_upwind_checksum(fdb_upwind* h, double* out) {
+  FDB_TRY(check_handle(h));
+  if (!out) return fail(FDB_ERR_INVALID, "null output");
+  FDB_TRY(launch_sum(h->buf[h->cur], h->g.ntot, h->part, h->dscal, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  *out = h->hscal[0];
+  return FDB_OK;
+}
+
+int fdb_upwind_std(fdb_upwind* h, double* out) {
+  FDB_TRY(check_handle(h));
+  if (!out) return fail(FDB_ERR_INVALID, "null output");
+  FDB_TRY(launch_std(h->buf[h->cur], h->g.ntot, h->part, h->dscal + 1, h->dscal, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  *out = h->hscal[0];
+  return FDB_OK;
+}
+
+int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream) {
+  FDB_TRY(check_handle(h));
+  FDB_TRY(sync(h));
+  h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own;
+  return FDB_OK;
+}
+
+int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth) {
+  FDB_TRY(check_handle(h));
+  if (arith < FDB_ARITH_AUTO || arith > FDB_ARITH_FIXED)
+    return fail(FDB_ERR_INVALID, "unknown arithmetic");
+  if (temporal_depth < 0 || temporal_depth > 16)
+    return fail(FDB_ERR_INVALID, "temporal_depth must be in [0, 16]");
+  h->arith = arith;
+  h->depth = temporal_depth;
+  return FDB_OK;
+}
+
+int fdb_upwind_info(fdb_upwind* h, uint64_t* ntot, int* arith_used) {
+  FDB_TRY(check_handle(h));
+  if (ntot) *ntot = h->g.ntot;
+  if (arith_used) *arith_used = h->arith_used;
+  return FDB_OK;
+}
+
+int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius, double noise_amp,
+                           uint64_t seed) {
+  FDB_TRY(check_handle(h));
+  if (!center) return fail(FDB_ERR_INVALID, "null centre");
+  FDB_TRY(launch_sphere_noise(h->g, center, radius, noise_amp, seed, h->buf[h->cur], h->stream));
+  return sync(h);
+}
+
+int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
+                            const double* lam_in_dev, double* lam_out_dev, double* dcoef_host) {
+  FDB_TRY(check_handle(h));
+  if (h->g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "adjoint serves ndims <= 3");
+  if (!f_dev || !lam_in_dev || !lam_out_dev) return fail(FDB_ERR_INVALID, "null buffer");
+  const Geom& g = h->g;
+  const Coeffs3 c = coeffs3(g, dt);
+  FDB_CUDA_TRY(cudaMemsetAsync(h->dpart, 0, 3 * adjoint_blocks() * sizeof(double), h->stream));
+  FDB_TRY(launch_adjoint_step(g, c, f_dev, lam_in_dev, lam_out_dev, h->dpart, h->stream));
+  FDB_TRY(launch_adjoint_finish(h->dpart, h->dscal, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  if (dcoef_host) {
+    const int jj[3] = {g.jz, g.jy, g.jx};
+    for (int k = 0; k < 3; ++k)
+      if (jj[k] >= 0) dcoef_host[jj[k]] += h->hscal[k];
+  }
+  return FDB_OK;
+}
+
+int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* lambda_T,
+                       double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
+  FDB_TRY(check_handle(h));
+  const Geom& g = h->g;
+  if (g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "adjoint serves ndims <= 3");
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  if (!lambda_T || !grad_f0) return fail(FDB_ERR_INVALID, "null lambda_T or grad_f0");
+  if (checkpoint_every < 0) return fail(FDB_ERR_INVALID, "checkpoint_every must be >= 0");
+  const int S = num_steps;
+  int K = checkpoint_every;
+  if (K == 0) K = std::max(1, (int)ceil(sqrt((double)std::max(S, 1))));
+  if (K > std::max(S, 1)) K = std::max(S, 1);
+  const int nseg = (S + K - 1) / K;
+  const size_t bytes = g.ntot * sizeof(double);
+  // The recompute must reproduce the forward states exactly, so the whole
+  // adjoint uses a per-step FP64 arithmetic (the fixed-point kernel only
+  // materialises every depth-th state).
+  const int arith = (h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA;
+
+  // storage: nseg checkpoints, K-1 segment states, two adjoint buffers
+  if ((int)h->ckpt.size() < nseg || (int)h->seg.size() < K - 1 || !h->lam[0]) {
+    free_adjoint(h);
+    h->ckpt.assign(nseg, nullptr);
+    h->seg.assign(std::max(K - 1, 0), nullptr);
+    int rc = FDB_OK;
+    for (auto& p : h->ckpt)
+      if (!rc) rc = dalloc(&p, g.ntot);
+    for (auto& p : h->seg)
+      if (!rc) rc = dalloc(&p, g.ntot);
+    if (!rc) rc = dalloc(&h->lam[0], g.ntot);
+    if (!rc) rc = dalloc(&h->lam[1], g.ntot);
+    if (rc) {
+      free_adjoint(h);
+      return rc;
+    }
+  }
+  const Coeffs3 c = coeffs3(g, dt);
+  // forward with checkpoints: ckpt[s] = f^{sK}
+  for (int s = 0; s < nseg; ++s) {
+    FDB_CUDA_TRY(cudaMemcpyAsync(h->ckpt[s], h->buf[h->cur], bytes, cudaMemcpyDeviceToDevice,
+                                 h->stream));
+    const int len = std::min(K, S - s * K);
+    FDB_TRY(advance(h, len, dt, arith));
+  }
+  // backward
+  int lc = 0;
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[lc], lambda_T, bytes,
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               h->stream));
+  FDB_CUDA_TRY(cudaMemsetAsync(h->dpart, 0, 3 * adjoint_blocks() * sizeof(double), h->stream));
+  for (int s = nseg - 1; s >= 0; --s) {
+    const int len = std::min(K, S - s * K);
+    // states f^{sK+1} .. f^{sK+len-1} into seg[0 .. len-2]
+    const double* prev = h->ckpt[s];
+    for (int k = 1; k < len; ++k) {
+      FDB_TRY(launch_step_f64(g, c, arith, prev, h->seg[k - 1], h->stream));
+      prev = h->seg[k - 1];
+    }
+    for (int k = len - 1; k >= 0; --k) {
+      const double* fk = (k == 0) ? h->ckpt[s] : h->seg[k - 1];
+      FDB_TRY(launch_adjoint_step(g, c, fk, h->lam[lc], h->lam[lc ^ 1], h->dpart, h->stream));
+      lc ^= 1;
+    }
+  }
+  FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], bytes,
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(launch_adjoint_finish(h->dpart, h->dscal, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  if (grad_v) {
+    // c_j = dt v_j up_j / dx_j  =>  dL/dv_j = dL/dc_j * dt up_j / dx_j
+    for (int j = 0; j < g.ndims; ++j) grad_v[j] = 0.0;
+    const int jj[3] = {g.jz, g.jy, g.jx};
+    for (int k = 0; k < 3; ++k)
+      if (jj[k] >= 0) grad_v[jj[k]] = h->hscal[k] * (dt * (double)g.up[jj[k]] / g.dx[jj[k]]);
+  }
+  return FDB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+// fdb_internal.h -- shared declarations of libfdb_upwind (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "fdb_upwind.h"
+
+namespace fdb {
+
+// Thread-local error message behind fdb_last_error().
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define FDB_CUDA_TRY(expr)                               \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return ::fdb::cuda_fail(_e, #expr); \
+  } while (0)
+
+#define FDB_TRY(expr)            \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != FDB_OK) return _rc; \
+  } while (0)
+
+// Host-side fault injection (env FDB_FAULT=alloc|launch|timeout|nan): lets the
+// failure paths be exercised without faulting a GPU.
+bool fault_injected(const char* kind);
+
+// Launch accounting behind fdb_launch_count(): every launch wrapper adds the
+// number of kernels it enqueued.
+void note_launch(uint64_t n = 1);
+
+// Geometry of one problem, normalised to 3 internal axes (z, y, x) = reference
+// axes (ndims-3, ndims-2, ndims-1); missing leading axes have extent 1 and
+// zero velocity.  Problems with more than 3 axes use the generic kernels.
+struct Geom {
+  int ndims = 0;
+  uint64_t n[FDB_MAX_DIMS] = {0};
+  double v[FDB_MAX_DIMS] = {0};
+  double L[FDB_MAX_DIMS] = {0};
+  double dx[FDB_MAX_DIMS] = {0};
+  int up[FDB_MAX_DIMS] = {0};
+  uint64_t dimProd[FDB_MAX_DIMS] = {0};
+  uint64_t ntot = 0;
+  // 3-D view (valid when ndims <= 3)
+  int64_t nz = 1, ny = 1, nx = 1;
+  int upz = -1, upy = -1, upx = -1;
+  int jz = -1, jy = -1, jx = -1;  // reference axis of each internal axis (-1: padded)
+};
+
+int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g);
+
+// The reference coefficient of axis j: ((dt * v_j) * up_j) / dx_j  (upwind.cxx:72).
+double ref_coeff(const Geom& g, int j, double dt);
+
+// Step coefficients in the 3-D view.  c* are the reference coefficients
+// (c <= 0); a* = -c* are the Courant numbers; w = ((1 - a_z) - a_y) - a_x.
+struct Coeffs3 {
+  double cz, cy, cx;
+  double az, ay, ax;
+  double w;
+};
+Coeffs3 coeffs3(const Geom& g, double dt);
+
+// ---- kernels (launch wrappers return FDB_OK or an error code) -------------
+int launch_step_f64(const Geom& g, const Coeffs3& c, int arith, const double* in,
+                    double* out, cudaStream_t s);
+int launch_step_generic(const Geom& g, double dt, const double* in, double* out,
+                        cudaStream_t s);
+
+// Temporally blocked block-fixed-point kernel: advances `steps` steps (a
+// multiple of nothing in particular; the wrapper splits into blocks of
+// `depth`).  Returns FDB_ERR_UNSUPPORTED when the geometry or coefficients
+// are outside what it serves (the caller then uses the FP64 kernel).
+int fixed_supported(const Geom& g, const Coeffs3& c, int depth);
+int launch_advect_fixed(const Geom& g, const Coeffs3& c, int steps, int depth,
+                        double** buf, int* cur, double* d_scratch, size_t scratch_bytes,
+                        cudaStream_t s);
+
+// Deterministic reductions.  `part` holds at least reduce_partials(n) doubles.
+uint32_t reduce_partials(uint64_t n);
+int launch_sum(const double* f, uint64_t n, double* part, double* d_out, cudaStream_t s);
+int launch_std(const double* f, uint64_t n, double* part, double* d_tmp2, double* d_out,
+               cudaStream_t s);
+
+int launch_fill_corner(double* f, uint64_t n, cudaStream_t s);
+int launch_sphere_noise(const Geom& g, const double* center, double radius, double amp,
+                        uint64_t seed, double* f, cudaStream_t s);
+
+// Adjoint step (3-D view): lam_out = A^T lam_in; dpart[3*G] accumulates the
+// per-block velocity-coefficient partials -<lam_in, S_j f - f>.
+uint32_t adjoint_blocks();
+int launch_adjoint_step(const Geom& g, const Coeffs3& c, const double* f,
+                        const double* lam_in, double* lam_out, double* dpart,
+                        cudaStream_t s);
+int launch_adjoint_finish(const double* dpart, double* d_out3, cudaStream_t s);
+
+}  // namespace fdb

@@ -1,0 +1,138 @@
+// upwindCxx -- the reference's benchmark driver (upwind/cxx/upwind.cxx:139-217)
+// on the GB300 library, through the C++ facade include/fidibench_gb/Upwind.h.
+//
+// Command line and output follow the reference so that its ctest cases
+// (upwind/cxx/CMakeLists.txt:54-91: `upwindCxx 32 10`, PASS_REGULAR_EXPRESSION
+// "[Cc]heck sum:[ ]*[1|0\.999]") run unchanged:
+//   -numCells <int> (128)  -numSteps <int> (10)  -vtk  -std  -h
+// Flags without a value toggle; tokens that are not options (such as the
+// positional "32 10" of the ctest cases) are ignored; an unknown -option prints
+// "<arg> is not a valid option." and the help text.  Added options:
+//   -arith <auto|exact|fma|fixed>  -courant <double> (0.1)  -json
+#include <cctype>
+#include <chrono>
+#include <cstdlib>
+#include <iostream>
+#include <limits>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fidibench_gb/Upwind.h"
+
+namespace {
+
+struct Options {
+  std::map<std::string, std::string> values;  // valued options
+  std::map<std::string, bool> flags;          // toggles
+  std::map<std::string, std::string> help;
+};
+
+bool is_option_name(const std::string& a) {
+  return a.size() >= 2 && a[0] == '-' && !std::isdigit((unsigned char)a[1]);
+}
+
+bool parse(Options& o, int argc, char** argv) {
+  for (int a = 1; a < argc; ++a) {
+    std::string arg(argv[a]);
+    if (is_option_name(arg) && !o.values.count(arg) && !o.flags.count(arg)) {
+      std::cout << arg << " is not a valid option.\n";
+      return false;
+    }
+  }
+  for (int a = 1; a < argc; ++a) {
+    std::string arg(argv[a]);
+    if (o.values.count(arg) && a + 1 < argc) o.values[arg] = argv[a + 1];
+    if (o.flags.count(arg)) o.flags[arg] = !o.flags[arg];
+  }
+  return true;
+}
+
+void print_help(const Options& o, const char* exe) {
+  std::cout << "Purpose: benchmark finite difference operations (GB300 library).\n";
+  std::cout << exe << " [options]\nUsage:\n";
+  for (const auto& kv : o.values)
+    std::cout << "\t" << kv.first << " <value> " << o.help.at(kv.first) << " (" << kv.second
+              << ")\n";
+  for (const auto& kv : o.flags)
+    std::cout << "\t" << kv.first << ' ' << o.help.at(kv.first) << " (" << kv.second << ")\n";
+}
+
+int arith_code(const std::string& s) {
+  if (s == "exact") return FDB_ARITH_EXACT;
+  if (s == "fma") return FDB_ARITH_FMA;
+  if (s == "fixed") return FDB_ARITH_FIXED;
+  return FDB_ARITH_AUTO;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  const int ndims = 3;
+  Options o;
+  o.values["-numCells"] = "128";
+  o.help["-numCells"] = "Number of cells along each axis";
+  o.values["-numSteps"] = "10";
+  o.help["-numSteps"] = "Number of time steps";
+  o.values["-arith"] = "auto";
+  o.help["-arith"] = "Step arithmetic: auto, exact, fma or fixed";
+  o.values["-courant"] = "0.1";
+  o.help["-courant"] = "Courant number used to pick dt";
+  o.flags["-vtk"] = false;
+  o.help["-vtk"] = "Write output to VTK file";
+  o.flags["-std"] = false;
+  o.help["-std"] = "Print out spread of solution";
+  o.flags["-json"] = false;
+  o.help["-json"] = "Print a JSON timing line";
+  o.flags["-h"] = false;
+  o.help["-h"] = "Print help.";
+
+  const bool success = parse(o, argc, argv);
+  if (!success || o.flags["-h"]) {
+    if (!success) std::cerr << "ERROR when parsing command line arguments\n";
+    print_help(o, argv[0]);
+    return 0;
+  }
+  const int numTimeSteps = std::atoi(o.values["-numSteps"].c_str());
+  const int n = std::atoi(o.values["-numCells"].c_str());
+  std::cout << "Running with CUDA enabled (" << fdb_version() << ")\n";
+
+  std::vector<size_t> numCells(ndims, (size_t)n);
+  std::cout << "number of cells: ";
+  for (size_t i = 0; i < numCells.size(); ++i) std::cout << ' ' << numCells[i];
+  std::cout << '\n';
+  std::cout << "number of time steps: " << numTimeSteps << '\n';
+
+  std::vector<double> velocity(numCells.size(), 1.0);
+  std::vector<double> lengths(numCells.size(), 1.0);
+  const double courant = std::atof(o.values["-courant"].c_str());
+  double dt = std::numeric_limits<double>::max();
+  for (size_t j = 0; j < velocity.size(); ++j) {
+    const double dx = lengths[j] / numCells[j];
+    const double val = courant * dx / velocity[j];
+    dt = (val < dt ? val : dt);
+  }
+
+  try {
+    Upwind<ndims> up(velocity, lengths, numCells);
+    up.setArith(arith_code(o.values["-arith"]));
+    if (o.flags["-vtk"]) up.saveVTK("up0.vtk");
+    const auto t0 = std::chrono::steady_clock::now();
+    up.advect(numTimeSteps, dt);
+    const double cs = up.checksum();
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::cout << "check sum: " << cs << '\n';
+    if (o.flags["-std"]) std::cout << "std      : " << up.std() << '\n';
+    if (o.flags["-vtk"]) up.saveVTK("up1.vtk");
+    if (o.flags["-json"]) {
+      const double cells = (double)n * n * n;
+      std::cout << "{\"cells\": " << cells << ", \"steps\": " << numTimeSteps
+                << ", \"seconds\": " << sec << ", \"gcups\": " << cells * numTimeSteps / sec / 1e9
+                << "}\n";
+    }
+  } catch (const std::exception& e) {
+    std::cerr << "ERROR: " << e.what() << '\n';
+    return 1;
+  }
+  return 0;
+}

@@ -1,0 +1,192 @@
+"""Python mirror of the reference's ``Upwind`` class, backed by libfdb_upwind.
+
+Mirrors upwind/python/upwind.py:8-86 (constructor arguments, ``advect``,
+``checksum``, ``printOut``, ``saveVTK``) and adds the C++ class's members
+(upwind/cxx/upwind.cxx:51-109: ``advect(numTimeSteps, deltaTime)``, ``std``,
+``print``).  All state lives on the GPU; host copies are made only when the
+caller asks for the field.
+
+Differences from the Python reference, by design:
+  * the field is advanced on the device by the CUDA step kernels; the
+    arithmetic is selectable (``arith="exact"`` reproduces the reference's
+    C++ operation order bit for bit, the default picks the fastest path that
+    meets the parity bar);
+  * ``f`` is a property: reading it copies the field to a numpy array,
+    assigning to it uploads a new field (setInitialCondition).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, lib
+
+
+def _as_u64(seq) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(seq, dtype=np.uint64))
+
+
+def _as_f64(seq) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(seq, dtype=np.float64))
+
+
+class Upwind:
+    """Periodic N-D first-order upwind advection of a scalar field (FP64)."""
+
+    def __init__(self, velocity, lengths, numCells, arith: str = "auto", depth: int = 0):
+        self.v = _as_f64(velocity)
+        self.lengths = _as_f64(lengths)
+        self.numCells = [int(x) for x in numCells]
+        self.ndims = len(self.numCells)
+        if not (len(self.v) == len(self.lengths) == self.ndims):
+            raise ValueError("velocity, lengths and numCells must have the same length")
+        n = _as_u64(self.numCells)
+        h = ctypes.c_void_p()
+        check(lib.fdb_upwind_create(self.ndims, self.v.ctypes.data, self.lengths.ctypes.data,
+                                    n.ctypes.data, ctypes.byref(h)))
+        self._h = h
+        self.ntot = int(np.prod(self.numCells))
+        # upwind/python/upwind.py:20-25
+        self.upDirection = np.where(self.v < 0.0, 1, -1).astype(np.int32)
+        self.deltas = self.lengths / np.asarray(self.numCells, dtype=np.float64)
+        self.set_arith(arith, depth)
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.fdb_upwind_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration ------------------------------------------------------------
+    def set_arith(self, arith: str = "auto", depth: int = 0) -> None:
+        code = _capi.ARITH_NAMES[arith] if isinstance(arith, str) else int(arith)
+        check(lib.fdb_upwind_set_arith(self._h, code, int(depth)))
+
+    def set_stream(self, stream) -> None:
+        """Enqueue on a CUDA stream (a torch.cuda.Stream, a raw handle or None)."""
+        raw = getattr(stream, "cuda_stream", stream)
+        check(lib.fdb_upwind_set_stream(self._h, raw))
+
+    @property
+    def arith_used(self) -> str:
+        ntot = ctypes.c_uint64()
+        a = ctypes.c_int()
+        check(lib.fdb_upwind_info(self._h, ctypes.byref(ntot), ctypes.byref(a)))
+        return {v: k for k, v in _capi.ARITH_NAMES.items()}.get(a.value, str(a.value))
+
+    # -- the reference API ----------------------------------------------------------
+    def advect(self, *args) -> None:
+        """``advect(deltaTime)`` (one step, upwind/python/upwind.py:46) or
+        ``advect(numTimeSteps, deltaTime)`` (upwind/cxx/upwind.cxx:51)."""
+        if len(args) == 1:
+            steps, dt = 1, args[0]
+        elif len(args) == 2:
+            steps, dt = args
+        else:
+            raise TypeError("advect(deltaTime) or advect(numTimeSteps, deltaTime)")
+        check(lib.fdb_upwind_advect(self._h, int(steps), float(dt)))
+
+    def checksum(self) -> float:
+        out = ctypes.c_double()
+        check(lib.fdb_upwind_checksum(self._h, ctypes.byref(out)))
+        return out.value
+
+    def std(self) -> float:
+        out = ctypes.c_double()
+        check(lib.fdb_upwind_std(self._h, ctypes.byref(out)))
+        return out.value
+
+    def printOut(self) -> None:
+        for i, x in enumerate(self.f):
+            print(i, " ", x)
+
+    def print(self) -> None:
+        for i, x in enumerate(self.f):
+            print(i, x)
+
+    def saveVTK(self, fname: str) -> None:
+        """ASCII rectilinear VTK file of the field (upwind/python/upwind.py:69-79)."""
+        from .vtk import write_rectilinear
+        write_rectilinear(fname, self.numCells, self.deltas, self.f, title="upwind")
+
+    # -- field access ------------------------------------------------------------
+    @property
+    def f(self) -> np.ndarray:
+        out = np.empty(self.ntot, dtype=np.float64)
+        check(lib.fdb_upwind_get_field(self._h, out.ctypes.data, 0))
+        return out
+
+    @f.setter
+    def f(self, values) -> None:
+        self.set_field(values)
+
+    def set_field(self, values) -> None:
+        """setInitialCondition: numpy array (host) or CUDA torch tensor (device)."""
+        if hasattr(values, "is_cuda") and values.is_cuda:
+            t = values.detach().to(dtype=__import__("torch").float64).contiguous()
+            if t.numel() != self.ntot:
+                raise ValueError(f"field has {t.numel()} values, expected {self.ntot}")
+            check(lib.fdb_upwind_set_field(self._h, t.data_ptr(), 1))
+            return
+        a = _as_f64(values).reshape(-1)
+        if a.size != self.ntot:
+            raise ValueError(f"field has {a.size} values, expected {self.ntot}")
+        check(lib.fdb_upwind_set_field(self._h, a.ctypes.data, 0))
+
+    def get_field(self, out=None):
+        """Copy the field into ``out`` (numpy or CUDA torch tensor) or a new array."""
+        if out is None:
+            return self.f
+        is_dev = 1 if getattr(out, "is_cuda", False) else 0
+        check(lib.fdb_upwind_get_field(self._h, _capi.dptr(out), is_dev))
+        return out
+
+    def field_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib.fdb_upwind_field_ptr(self._h, ctypes.byref(p)))
+        return p.value
+
+    def init_sphere(self, center, radius: float, noise_amp: float = 0.0, seed: int = 0) -> None:
+        c = _as_f64(center)
+        if c.size != self.ndims:
+            raise ValueError("centre needs one coordinate per axis")
+        check(lib.fdb_upwind_init_sphere(self._h, c.ctypes.data, float(radius), float(noise_amp),
+                                         int(seed)))
+
+    # -- adjoint -------------------------------------------------------------------
+    def adjoint(self, numTimeSteps: int, deltaTime: float, lambda_T, grad_f0=None,
+                checkpoint_every: int = 0):
+        """Gradient of a loss L(f_T) given lambda_T = dL/df_T.
+
+        Runs the forward steps from the current field (which ends at f_T) and
+        the transposed steps backward with checkpoint/recompute.  Returns
+        (grad_f0, grad_v).  lambda_T/grad_f0 may be numpy arrays or CUDA
+        tensors (both of the same kind)."""
+        is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
+        if grad_f0 is None:
+            if is_dev:
+                import torch
+                grad_f0 = torch.empty(self.ntot, dtype=torch.float64, device=lambda_T.device)
+            else:
+                grad_f0 = np.empty(self.ntot, dtype=np.float64)
+        if not is_dev:
+            lambda_T = _as_f64(lambda_T).reshape(-1)
+        gv = np.zeros(self.ndims, dtype=np.float64)
+        check(lib.fdb_upwind_adjoint(self._h, int(numTimeSteps), float(deltaTime),
+                                     _capi.dptr(lambda_T), _capi.dptr(grad_f0), gv.ctypes.data,
+                                     int(checkpoint_every), is_dev))
+        return grad_f0, gv

@@ -1,0 +1,146 @@
+/*
+ * fdb_upwind.h -- C-ABI of the GB300-native upwind advection library
+ * (libfdb_upwind.so).  Plain C types only: pointers, sizes and status codes.
+ *
+ * The reference has no FFI of its own: its interface is the class template
+ * Upwind<NDIMS> defined inside the driver translation unit
+ * upwind/cxx/upwind.cxx:19-135.  Each entry point below names the member it
+ * replaces.  include/fidibench_gb/Upwind.h rebuilds that class on top of
+ * these calls with the reference's exact signatures, and
+ * fidibench_gb300/upwind.py mirrors the Python class of
+ * upwind/python/upwind.py:8-86.
+ *
+ * Conventions
+ *  - Every call returns FDB_OK (0) or a positive FDB_ERR_* code;
+ *    fdb_last_error() returns a thread-local message for the last failure.
+ *  - Fields are FP64, row-major with the LAST index varying fastest
+ *    (upwind.cxx:39-44).  Axis j uses the upwind neighbour i_j + up_j with
+ *    up_j = -1 for v_j >= 0 and +1 for v_j < 0 (upwind.cxx:34-35), periodic.
+ *  - A handle owns its device buffers and one CUDA stream.  Handles are not
+ *    thread-safe; distinct handles are independent.
+ *  - `is_device` = 1 means the pointer is device memory of the handle's GPU
+ *    (e.g. a torch CUDA tensor's data_ptr()); 0 means host memory.
+ *  - Calls that return data to the host synchronise the handle's stream.
+ */
+#ifndef FDB_UPWIND_H
+#define FDB_UPWIND_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDB_OK 0
+#define FDB_ERR_INVALID 1      /* bad argument (sizes, dims, null pointers)    */
+#define FDB_ERR_CUDA 2         /* a CUDA runtime call or kernel launch failed  */
+#define FDB_ERR_ALLOC 3        /* device or pinned allocation failed           */
+#define FDB_ERR_UNSUPPORTED 4  /* valid request that this build does not serve */
+#define FDB_ERR_TIMEOUT 5      /* a bounded device-side wait gave up           */
+#define FDB_ERR_NONFINITE 6    /* finiteness check found a NaN/Inf             */
+#define FDB_ERR_INJECTED 7     /* host-side fault injection (FDB_FAULT)        */
+
+#define FDB_MAX_DIMS 8
+
+/* Arithmetic of the step kernel (fdb_upwind_set_arith).
+ *  FDB_ARITH_EXACT : the reference's operation order with every FP64
+ *                    operation separately rounded (upwind.cxx:72,80): the
+ *                    field is bit-identical to the reference built without
+ *                    FMA contraction.
+ *  FDB_ARITH_FMA   : FP64 in the minimal form w*f + sum_j a_j*f_up_j
+ *                    (1 DMUL + 3 DFMA per cell-update).
+ *  FDB_ARITH_FIXED : temporally blocked kernel that carries the field in
+ *                    64-bit block-fixed-point between one FP64 load and one
+ *                    FP64 store per block of steps (integer pipes instead of
+ *                    the FP64 pipe).
+ *  FDB_ARITH_AUTO  : FIXED where the geometry allows it, else FMA (default). */
+#define FDB_ARITH_AUTO 0
+#define FDB_ARITH_EXACT 1
+#define FDB_ARITH_FMA 2
+#define FDB_ARITH_FIXED 3
+
+typedef struct fdb_upwind fdb_upwind;
+
+/* Replaces Upwind(velocity, lengths, numCells)  -- upwind/cxx/upwind.cxx:23-49.
+ * Allocates the field on the current CUDA device and sets f = 0, f[0] = 1
+ * like the reference constructor (:45-48).  ndims in [1, FDB_MAX_DIMS]. */
+int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
+                      const uint64_t* num_cells, fdb_upwind** out);
+
+/* Replaces ~Upwind (implicit; std::vector members freed). */
+int fdb_upwind_destroy(fdb_upwind* h);
+
+/* setInitialCondition: overwrite f with ntot values (upwind.cxx:45-48 is the
+ * reference's hard-coded initial condition; this replaces it). */
+int fdb_upwind_set_field(fdb_upwind* h, const double* src, int is_device);
+
+/* Copy f out (the reference exposes f only through print()/saveVTK(),
+ * upwind.cxx:105-109 and saveVTK.h:1-60). */
+int fdb_upwind_get_field(fdb_upwind* h, double* dst, int is_device);
+
+/* Device address of the current field (valid until the next advect/set). */
+int fdb_upwind_field_ptr(fdb_upwind* h, double** out);
+
+/* Replaces advect(int numTimeSteps, double deltaTime) -- upwind.cxx:51-86.
+ * Enqueued on the handle's stream; does not synchronise. */
+int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt);
+
+/* Replaces checksum() -- upwind.cxx:91-93 (sum of f, no cell volume).
+ * Deterministic fixed-order tree sum on the device; synchronises. */
+int fdb_upwind_checksum(fdb_upwind* h, double* out);
+
+/* Replaces std() -- upwind.cxx:95-103 (population standard deviation). */
+int fdb_upwind_std(fdb_upwind* h, double* out);
+
+/* Stream to enqueue on (a cudaStream_t; NULL restores the handle's own). */
+int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream);
+
+/* Select the step arithmetic (FDB_ARITH_*) and the temporal block depth of
+ * the FIXED kernel (0 = autotuned/default). */
+int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
+
+/* Number of cells, and the arithmetic the last advect actually used. */
+int fdb_upwind_info(fdb_upwind* h, uint64_t* ntot, int* arith_used);
+
+/* Synthetic initial condition on the device: 1 inside the sphere of the given
+ * centre/radius (cell centres (i+0.5)*dx), 0 outside, plus noise_amp*U[0,1)
+ * from a counter-based SplitMix64 stream keyed by (seed, flat index).  The
+ * reference has no such call (its IC is hard-coded, upwind.cxx:48). */
+int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius,
+                           double noise_amp, uint64_t seed);
+
+/* ---------------------------------------------------------------------------
+ * Adjoint (no reference counterpart; the transpose of advect()).
+ * Runs advect(num_steps, dt) forward from the handle's current field f0,
+ * storing a checkpoint every `checkpoint_every` steps (0 = sqrt(num_steps)),
+ * then runs the transposed step backward from lambda_T = dL/df_T, recomputing
+ * each segment from its checkpoint.  Writes grad_f0 = dL/df0 (ntot values)
+ * and grad_v = dL/dv (ndims values, host memory).  The handle's field is left
+ * at f_T (as after advect).  Pointers are device memory when is_device = 1.
+ * ------------------------------------------------------------------------- */
+int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
+                       const double* lambda_T, double* grad_f0, double* grad_v,
+                       int checkpoint_every, int is_device);
+
+/* One transposed step on caller buffers (device pointers):
+ * lam_out = A^T lam_in, and dcoef[j] += -<lam_in, S_j f - f> (host array).
+ * Used by tests and by callers that manage their own checkpoints. */
+int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
+                            const double* lam_in_dev, double* lam_out_dev,
+                            double* dcoef_host);
+
+/* Number of kernels this library has launched in this process (all handles,
+ * all threads).  A diagnostic for benchmarks; no reference counterpart. */
+uint64_t fdb_launch_count(void);
+
+/* Thread-local message for the last non-zero status. */
+const char* fdb_last_error(void);
+
+/* Library version string. */
+const char* fdb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDB_UPWIND_H */

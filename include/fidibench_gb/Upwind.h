@@ -1,0 +1,147 @@
+// Upwind.h -- the reference's C++ class Upwind<NDIMS> (upwind/cxx/upwind.cxx:19-135)
+// rebuilt on the C-ABI of libfdb_upwind (include/fdb_upwind.h).
+//
+// Same constructor and member signatures as the reference, so a driver written
+// against upwind.cxx compiles against this header unchanged:
+//   Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
+//          const std::vector<size_t>& numCells)                 upwind.cxx:23-49
+//   void   advect(int numTimeSteps, double deltaTime)           upwind.cxx:51-86
+//   void   saveVTK(const std::string& filename)                 saveVTK.h:1-60
+//   double checksum() const                                     upwind.cxx:91-93
+//   double std() const                                          upwind.cxx:95-103
+//   void   print() const                                        upwind.cxx:105-109
+// Additions: setInitialCondition(), getField(), setArith(), handle().
+//
+// Differences, by design: the field lives on the GPU (copied to the host only
+// by print/saveVTK/getField); errors throw std::runtime_error carrying
+// fdb_last_error() (the reference has no error reporting); advect() returns
+// once the work is enqueued and the next host-visible call synchronises.
+#ifndef FIDIBENCH_GB_UPWIND_H
+#define FIDIBENCH_GB_UPWIND_H
+
+#include <cstddef>
+#include <cstdint>
+#include <fstream>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../fdb_upwind.h"
+
+namespace fdb {
+
+inline void check(int rc, const char* what) {
+  if (rc != FDB_OK)
+    throw std::runtime_error(std::string(what) + " failed (" + std::to_string(rc) +
+                             "): " + fdb_last_error());
+}
+
+template <size_t NDIMS>
+class Upwind {
+ public:
+  Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
+         const std::vector<size_t>& numCells)
+      : v_(velocity), lengths_(lengths), numCells_(numCells) {
+    if (velocity.size() < NDIMS || lengths.size() < NDIMS || numCells.size() < NDIMS)
+      throw std::invalid_argument("Upwind: need NDIMS velocity, lengths and numCells entries");
+    std::vector<uint64_t> n(numCells.begin(), numCells.begin() + NDIMS);
+    check(fdb_upwind_create((int)NDIMS, velocity.data(), lengths.data(), n.data(), &h_),
+          "fdb_upwind_create");
+    ntot_ = 1;
+    for (size_t j = 0; j < NDIMS; ++j) {
+      deltas_.push_back(lengths[j] / numCells[j]);
+      ntot_ *= numCells[j];
+    }
+  }
+  ~Upwind() { fdb_upwind_destroy(h_); }
+  Upwind(const Upwind&) = delete;
+  Upwind& operator=(const Upwind&) = delete;
+
+  void advect(int numTimeSteps, double deltaTime) {
+    check(fdb_upwind_advect(h_, numTimeSteps, deltaTime), "fdb_upwind_advect");
+  }
+
+  double checksum() const {
+    double s = 0.0;
+    check(fdb_upwind_checksum(h_, &s), "fdb_upwind_checksum");
+    return s;
+  }
+
+  double std() const {
+    double s = 0.0;
+    check(fdb_upwind_std(h_, &s), "fdb_upwind_std");
+    return s;
+  }
+
+  void print() const {
+    std::vector<double> f = getField();
+    for (size_t i = 0; i < f.size(); ++i) std::cout << i << " " << f[i] << '\n';
+  }
+
+  // ASCII RECTILINEAR_GRID, the reference writer's layout (saveVTK.h:1-60).
+  void saveVTK(const std::string& filename) {
+    std::vector<double> f = getField();
+    std::fstream file;
+    file.open(filename.c_str(), std::ios_base::out);
+    file << "# vtk DataFile Version 2.0\nupwind.cxx\nASCII\nDATASET RECTILINEAR_GRID\n";
+    file << "DIMENSIONS";
+    file << ' ' << (NDIMS > 2 ? numCells_[NDIMS > 2 ? 2 : 0] + 1 : 1);
+    file << ' ' << (NDIMS > 1 ? numCells_[NDIMS > 1 ? 1 : 0] + 1 : 1);
+    file << ' ' << numCells_[0] + 1;
+    axis(file, "X_COORDINATES", NDIMS > 2 ? 2 : -1);
+    axis(file, "Y_COORDINATES", NDIMS > 1 ? 1 : -1);
+    axis(file, "Z_COORDINATES", 0);
+    file << "\nCELL_DATA " << ntot_ << '\n';
+    file << "SCALARS f double 1\nLOOKUP_TABLE default\n";
+    for (size_t i = 0; i < ntot_; ++i) {
+      file << f[i] << " ";
+      if ((i + 1) % 10 == 0) file << '\n';
+    }
+    file << '\n';
+  }
+
+  // setInitialCondition: replaces the constructor's f = 0, f[0] = 1.
+  void setInitialCondition(const std::vector<double>& f) {
+    if (f.size() != ntot_) throw std::invalid_argument("setInitialCondition: wrong size");
+    check(fdb_upwind_set_field(h_, f.data(), 0), "fdb_upwind_set_field");
+  }
+
+  std::vector<double> getField() const {
+    std::vector<double> f(ntot_);
+    check(fdb_upwind_get_field(h_, f.data(), 0), "fdb_upwind_get_field");
+    return f;
+  }
+
+  void setArith(int arith, int temporalDepth = 0) {
+    check(fdb_upwind_set_arith(h_, arith, temporalDepth), "fdb_upwind_set_arith");
+  }
+
+  fdb_upwind* handle() { return h_; }
+  size_t size() const { return ntot_; }
+
+ private:
+  void axis(std::fstream& file, const char* label, int k) const {
+    file << "\n" << label << " ";
+    if (k < 0) {
+      file << "1 double\n0.0\n";
+      return;
+    }
+    file << numCells_[k] + 1 << " double\n";
+    for (size_t i = 0; i < numCells_[k] + 1; ++i) file << ' ' << 0.0 + deltas_[k] * i;
+  }
+
+  fdb_upwind* h_ = nullptr;
+  std::vector<double> v_, lengths_, deltas_;
+  std::vector<size_t> numCells_;
+  size_t ntot_ = 0;
+};
+
+}  // namespace fdb
+
+#ifndef FDB_NO_GLOBAL_UPWIND
+// Drop-in: code written against the reference's global Upwind<NDIMS>.
+using fdb::Upwind;
+#endif
+
+#endif  // FIDIBENCH_GB_UPWIND_H

@@ -1,0 +1,203 @@
+"""ctypes front-end of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/_build/libfdb_oracle.so`` (the C restatement of
+upwind/cxx/upwind.cxx:51-103, see upwind_oracle.c) and, when it was built in
+this tree, ``oracle/_ref/libfdb_refupwind.so`` (the reference's own
+upwind.cxx compiled by path).  Only tests/, ``__graft_entry__.smoke()`` and
+bench.py's CPU-baseline / reference legs import this module; the product
+package never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libfdb_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libfdb_refupwind.so")
+REF_EXE = os.path.join(HERE, "_ref", "upwindCxx")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the restatement (always) and the reference harness (when the
+    reference source tree is present) with oracle/Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    refdir = os.environ.get("FDB_REFERENCE_DIR", "/root/reference")
+    if ref is None:
+        ref = os.path.isfile(os.path.join(refdir, "upwind", "cxx", "upwind.cxx"))
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _u64(seq) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(seq, dtype=np.uint64))
+
+
+def _f64(seq) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(seq, dtype=np.float64))
+
+
+class Port:
+    """The C restatement (upwind_oracle.c)."""
+
+    def __init__(self, path: str = PORT_SO):
+        if not os.path.isfile(path):
+            build(ref=False)
+        lib = ctypes.CDLL(path)
+        lib.fdbo_advect.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp, _dp,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        lib.fdbo_advect.restype = ctypes.c_int
+        lib.fdbo_checksum.argtypes = [_dp, ctypes.c_uint64]
+        lib.fdbo_checksum.restype = ctypes.c_double
+        lib.fdbo_std.argtypes = [_dp, ctypes.c_uint64]
+        lib.fdbo_std.restype = ctypes.c_double
+        lib.fdbo_coeff.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        lib.fdbo_coeff.restype = ctypes.c_double
+        lib.fdbo_adjoint_step.argtypes = [ctypes.c_int, _u64p, _dp, _dp, ctypes.c_double,
+                                          _dp, _dp, _dp, _dp]
+        lib.fdbo_adjoint_step.restype = ctypes.c_int
+        lib.fdbo_fill_sphere_noise.argtypes = [ctypes.c_int, _u64p, _dp, _dp, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_uint64, _dp]
+        lib.fdbo_fill_sphere_noise.restype = ctypes.c_int
+        lib.fdbo_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        lib.fdbo_uniform.restype = ctypes.c_double
+        lib.fdbo_max_threads.restype = ctypes.c_int
+        self.lib = lib
+
+    def advect(self, n, v, L, f0, steps: int, dt: float, threads: int = 0) -> np.ndarray:
+        return self.advect_timed(n, v, L, f0, steps, dt, threads)[0]
+
+    def advect_timed(self, n, v, L, f0, steps: int, dt: float, threads: int = 0):
+        """(final field, wall seconds of the advect call alone)."""
+        import time
+        n, v, L = _u64(n), _f64(v), _f64(L)
+        f = np.array(f0, dtype=np.float64, copy=True).reshape(-1)
+        scratch = np.empty_like(f)
+        scratch.fill(0.0)  # fault the pages in outside the timed call
+        t0 = time.perf_counter()
+        rc = self.lib.fdbo_advect(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                  _ptr(f), _ptr(scratch), int(steps), float(dt), int(threads))
+        el = time.perf_counter() - t0
+        if rc:
+            raise ValueError("oracle advect rejected its arguments")
+        return f, el
+
+    def checksum(self, f) -> float:
+        f = _f64(f).reshape(-1)
+        return self.lib.fdbo_checksum(_ptr(f), f.size)
+
+    def std(self, f) -> float:
+        f = _f64(f).reshape(-1)
+        return self.lib.fdbo_std(_ptr(f), f.size)
+
+    def adjoint_step(self, n, v, L, dt, f, lam_in):
+        """Returns (lam_out, dcoef[ndims]) for one transposed step."""
+        n, v, L = _u64(n), _f64(v), _f64(L)
+        f = _f64(f).reshape(-1)
+        lam_in = _f64(lam_in).reshape(-1)
+        lam_out = np.empty_like(lam_in)
+        dcoef = np.zeros(len(n), dtype=np.float64)
+        rc = self.lib.fdbo_adjoint_step(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                        float(dt), _ptr(f), _ptr(lam_in), _ptr(lam_out),
+                                        _ptr(dcoef))
+        if rc:
+            raise ValueError("oracle adjoint rejected its arguments")
+        return lam_out, dcoef
+
+    def sphere_noise(self, n, L, center, radius, noise_amp, seed) -> np.ndarray:
+        n, L, c = _u64(n), _f64(L), _f64(center)
+        f = np.empty(int(np.prod(n)), dtype=np.float64)
+        rc = self.lib.fdbo_fill_sphere_noise(len(n), n.ctypes.data_as(_u64p), _ptr(L), _ptr(c),
+                                             float(radius), float(noise_amp), int(seed), _ptr(f))
+        if rc:
+            raise ValueError("oracle sphere_noise rejected its arguments")
+        return f
+
+    def max_threads(self) -> int:
+        return self.lib.fdbo_max_threads()
+
+
+class Reference:
+    """The reference's own Upwind<NDIMS> (ref_harness.cpp), when built here."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.isfile(path):
+            raise FileNotFoundError(path)
+        lib = ctypes.CDLL(path)
+        lib.fdbr_advect.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp, _dp,
+                                    ctypes.c_int, ctypes.c_double, _dp]
+        lib.fdbr_advect.restype = ctypes.c_int
+        lib.fdbr_default_field.argtypes = [ctypes.c_int, _u64p, _dp]
+        lib.fdbr_default_field.restype = ctypes.c_int
+        lib.fdbr_checksum.argtypes = [ctypes.c_int, _u64p, _dp]
+        lib.fdbr_checksum.restype = ctypes.c_double
+        lib.fdbr_std.argtypes = [ctypes.c_int, _u64p, _dp]
+        lib.fdbr_std.restype = ctypes.c_double
+        self.lib = lib
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.isfile(REF_SO)
+
+    def advect(self, n, v, L, f0, steps: int, dt: float) -> np.ndarray:
+        return self.advect_timed(n, v, L, f0, steps, dt)[0]
+
+    def advect_timed(self, n, v, L, f0, steps: int, dt: float):
+        """(final field, wall seconds of the reference's advect() call alone)."""
+        n, v, L = _u64(n), _f64(v), _f64(L)
+        out = np.empty(int(np.prod(n)), dtype=np.float64)
+        fin = None if f0 is None else _f64(f0).reshape(-1)
+        sec = ctypes.c_double(0.0)
+        rc = self.lib.fdbr_advect(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                  None if fin is None else _ptr(fin), _ptr(out),
+                                  int(steps), float(dt), ctypes.byref(sec))
+        if rc:
+            raise ValueError("reference harness rejected its arguments")
+        return out, sec.value
+
+    def default_field(self, n) -> np.ndarray:
+        n = _u64(n)
+        out = np.empty(int(np.prod(n)), dtype=np.float64)
+        self.lib.fdbr_default_field(len(n), n.ctypes.data_as(_u64p), _ptr(out))
+        return out
+
+    def checksum(self, n, f) -> float:
+        n = _u64(n)
+        f = _f64(f).reshape(-1)
+        return self.lib.fdbr_checksum(len(n), n.ctypes.data_as(_u64p), _ptr(f))
+
+    def std(self, n, f) -> float:
+        n = _u64(n)
+        f = _f64(f).reshape(-1)
+        return self.lib.fdbr_std(len(n), n.ctypes.data_as(_u64p), _ptr(f))
+
+
+def reference_dt(n, v, L, courant: float) -> float:
+    """dt = min_j courant * dx_j / v_j as the reference driver computes it
+    (upwind/cxx/upwind.cxx:186-192, which assumes v_j > 0)."""
+    dt = np.finfo(np.float64).max
+    for nj, vj, Lj in zip(n, v, L):
+        dx = float(Lj) / float(nj)
+        val = courant * dx / float(vj)
+        dt = val if val < dt else dt
+    return dt
+
+
+def cfl_dt(n, v, L, cfl: float) -> float:
+    """dt = cfl * min_j dx_j / |v_j| (axes with v_j = 0 are skipped), the rule
+    the synthetic workloads use for signed velocities."""
+    dt = np.inf
+    for nj, vj, Lj in zip(n, v, L):
+        if vj != 0.0:
+            dt = min(dt, cfl * (float(Lj) / float(nj)) / abs(float(vj)))
+    return float(dt if np.isfinite(dt) else cfl)

@@ -1,0 +1,139 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+    python tests/golden/make_golden.py
+
+Runs the reference's own Upwind<NDIMS> (upwind/cxx/upwind.cxx, compiled by
+oracle/Makefile target `ref` from the reference tree, no FMA contraction) and
+the reference's Python Upwind (upwind/python/upwind.py, imported from the
+reference tree) on small seeded inputs, and stores inputs and outputs as
+.npz files.  The reference tree is read only by this script; the tests read
+the committed .npz files, so they also run where the reference is absent.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import Port, Reference, build, cfl_dt, reference_dt  # noqa: E402
+
+REFDIR = os.environ.get("FDB_REFERENCE_DIR", "/root/reference")
+SEED = 20261203
+
+
+def save(name: str, **arrays) -> None:
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print("wrote", os.path.relpath(path, ROOT), os.path.getsize(path), "bytes")
+
+
+def field_cases(ref: Reference, port: Port) -> None:
+    rng = np.random.default_rng(SEED)
+    cases = [
+        # name, n, v, L, steps, cfl, init
+        ("g3_7x5x6_mixed", (7, 5, 6), (1.0, -0.7, 0.3), (1.0, 1.0, 1.0), 13, 0.5, "uniform"),
+        ("g3_8x8x8_c1sphere", (8, 8, 8), (1.0, 1.0, 1.0), (1.0, 1.0, 1.0), 10, 0.5, "sphere"),
+        ("g3_5x9x4_negall", (5, 9, 4), (-0.9, -0.2, -1.0), (2.0, 0.5, 1.0), 21, 0.45, "uniform"),
+        ("g3_1x6x3_zerov", (1, 6, 3), (0.0, 0.6, -0.0), (1.0, 1.0, 1.0), 7, 0.5, "signed"),
+        ("g3_3x3x3_c2noise", (3, 3, 3), (1.0, -0.7, 0.3), (1.0, 1.0, 1.0), 100, 0.5, "sphere_noise"),
+        ("g2_9x11", (9, 11), (-0.4, 0.9), (1.0, 1.0), 17, 0.5, "uniform"),
+        ("g1_17", (17,), (-1.3,), (1.0,), 9, 0.8, "signed"),
+        ("g4_3x4x5x6", (3, 4, 5, 6), (0.1, -0.2, 0.3, -0.4), (1.0, 1.0, 1.0, 1.0), 5, 0.5,
+         "uniform"),
+    ]
+    for name, n, v, L, steps, cfl, init in cases:
+        ntot = int(np.prod(n))
+        if init == "uniform":
+            f0 = rng.random(ntot)
+        elif init == "signed":
+            f0 = rng.standard_normal(ntot)
+        elif init == "sphere":
+            f0 = port.sphere_noise(n, L, [0.5 * x for x in L], 0.2 * min(L), 0.0, 0)
+        else:
+            f0 = port.sphere_noise(n, L, [0.5 * x for x in L], 0.2 * min(L), 0.01, SEED)
+        dt = cfl_dt(n, v, L, cfl)
+        fT = ref.advect(n, v, L, f0, steps, dt)
+        save(name, n=np.asarray(n, np.uint64), v=np.asarray(v, np.float64),
+             L=np.asarray(L, np.float64), dt=np.float64(dt), steps=np.int64(steps), f0=f0, fT=fT,
+             checksum=np.float64(ref.checksum(n, fT)), std=np.float64(ref.std(n, fT)))
+
+
+def driver_cases(ref: Reference) -> None:
+    """The reference driver's own run (upwind.cxx:139-217): corner IC, v = 1,
+    L = 1, courant 0.1, for the ctest size (128^3 x 10) and 32^3 x 10."""
+    for N in (32, 128):
+        n = (N, N, N)
+        v = (1.0, 1.0, 1.0)
+        L = (1.0, 1.0, 1.0)
+        dt = reference_dt(n, v, L, 0.1)
+        fT = ref.advect(n, v, L, None, 10, dt)
+        idx = np.array([0, 1, 2, N, N * N, N * N + N + 1, 10, 11 * N * N, N ** 3 - 1],
+                       dtype=np.int64)
+        save(f"driver_{N}cube_10", n=np.asarray(n, np.uint64), dt=np.float64(dt),
+             steps=np.int64(10), idx=idx, values=fT[idx], checksum=np.float64(ref.checksum(n, fT)),
+             std=np.float64(ref.std(n, fT)), nonzero=np.int64(np.count_nonzero(fT)))
+
+
+def python_reference_case() -> None:
+    """The reference's Python Upwind (upwind/python/upwind.py), 12^3 x 10."""
+    pydir = os.path.join(REFDIR, "upwind", "python")
+    sys.path.insert(0, pydir)
+    try:
+        import upwind as pyup  # the reference module
+    finally:
+        sys.path.remove(pydir)
+    n = [12, 12, 12]
+    v = np.ones(3)
+    L = np.ones(3)
+    dt = reference_dt(n, v, L, 0.1)
+    up = pyup.Upwind(v, L, n)
+    for _ in range(10):
+        up.advect(dt)
+    save("python_12cube_10", n=np.asarray(n, np.uint64), dt=np.float64(dt), steps=np.int64(10),
+         fT=up.f.copy(), checksum=np.float64(up.checksum()))
+
+
+def vtk_case() -> None:
+    """The reference driver binary (oracle/_ref/upwindCxx, built from the
+    reference's own upwind.cxx + CmdLineArgParser.cpp) with -vtk -std: its
+    stdout and up1.vtk for 6^3 x 3 steps."""
+    import subprocess
+    import tempfile
+    exe = os.path.join(ROOT, "oracle", "_ref", "upwindCxx")
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([exe, "-numCells", "6", "-numSteps", "3", "-vtk", "-std"], cwd=d,
+                           capture_output=True, text=True, check=True,
+                           env=dict(os.environ, OMP_NUM_THREADS="2"))
+        vtk = open(os.path.join(d, "up1.vtk")).read()
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith(("check sum", "std", "number of"))]
+    save("driver_vtk_6cube_3", up1_vtk=np.array(vtk), stdout=np.array("\n".join(lines)))
+
+
+def synth_case(port: Port) -> None:
+    """Pins the synthetic sphere+noise generator (no reference counterpart)."""
+    n = (16, 12, 10)
+    L = (1.0, 1.0, 1.0)
+    f = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.2, 0.01, SEED)
+    u = np.array([port.lib.fdbo_uniform(SEED, i) for i in range(8)])
+    save("synth_sphere_16x12x10", n=np.asarray(n, np.uint64), f=f, uniform8=u,
+         seed=np.uint64(SEED))
+
+
+def main() -> None:
+    build(ref=True)
+    ref = Reference()
+    port = Port()
+    field_cases(ref, port)
+    driver_cases(ref)
+    python_reference_case()
+    vtk_case()
+    synth_case(port)
+
+
+if __name__ == "__main__":
+    main()

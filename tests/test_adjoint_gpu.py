@@ -1,0 +1,115 @@
+"""Adjoint (transposed step + checkpoint/recompute) through the C-ABI:
+agreement with the oracle's transposed step, the dot-product identity
+<A x, y> = <x, A^T y>, and central finite differences (h = 1e-6) of
+L = 0.5 ||f_T - target||^2 with respect to f0 and the velocity."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_maxnorm
+
+pytestmark = pytest.mark.gpu
+
+FD_TOL = 1e-6
+
+
+def test_adjoint_step_matches_oracle(fdb, port):
+    import torch
+    n, L = (9, 10, 11), (1.0, 1.0, 1.0)
+    rng = np.random.default_rng(2)
+    for v in [(1.0, -0.7, 0.3), (-0.5, 0.5, -0.5), (0.2, 0.0, 1.0)]:
+        dt = 0.4 / 11
+        f = rng.standard_normal(990)
+        lam = rng.standard_normal(990)
+        ref_lam, ref_dc = port.adjoint_step(n, v, L, dt, f, lam)
+        up = fdb.Upwind(v, L, n)
+        fd = torch.tensor(f, device="cuda")
+        ld = torch.tensor(lam, device="cuda")
+        out = torch.empty_like(ld)
+        dc = np.zeros(3)
+        from fidibench_gb300._capi import check, lib
+        check(lib.fdb_upwind_adjoint_step(up._h, dt, fd.data_ptr(), ld.data_ptr(),
+                                          out.data_ptr(), dc.ctypes.data))
+        assert rel_maxnorm(out.cpu().numpy(), ref_lam) <= 1e-14
+        assert np.allclose(dc, ref_dc, rtol=1e-12, atol=1e-12 * np.abs(ref_dc).max())
+        up.close()
+
+
+@pytest.mark.parametrize("v,ckpt", [((1.0, -0.7, 0.3), 0), ((0.8, 0.5, -0.6), 7),
+                                    ((-0.3, -0.9, 0.6), 1), ((0.5, 0.5, 0.5), 50)])
+def test_dot_product_identity(fdb, v, ckpt):
+    n, L = (24, 20, 28), (1.0, 1.0, 1.0)
+    steps = 37
+    dt = 0.5 / 28
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(int(np.prod(n)))
+    y = rng.standard_normal(int(np.prod(n)))
+    up = fdb.Upwind(v, L, n)
+    up.f = x
+    up.advect(steps, dt)
+    ax = up.f
+    up.f = x
+    aty, _ = up.adjoint(steps, dt, y, checkpoint_every=ckpt)
+    assert np.allclose(up.f, ax, rtol=0, atol=1e-13 * np.abs(ax).max())
+    lhs, rhs = float(ax @ y), float(x @ aty)
+    assert lhs == pytest.approx(rhs, rel=1e-11)
+    up.close()
+
+
+def _fd_diff(fp, fm, target, h):
+    rp, rm = fp - target, fm - target
+    return float(np.sum((rp - rm) * (rp + rm))) / (4.0 * h)
+
+
+def _forward(fdb, v, L, n, f0, steps, dt):
+    up = fdb.Upwind(v, L, n, arith="fma")
+    up.f = f0
+    up.advect(steps, dt)
+    out = up.f
+    up.close()
+    return out
+
+
+def test_finite_differences(fdb, port):
+    n, L = (32, 24, 40), (1.0, 1.0, 1.0)
+    v = np.array([0.8, 0.5, -0.6])
+    steps, dt = 60, 0.5 / 40
+    rng = np.random.default_rng(8)
+    f0 = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.25, 0.01, 1)
+    target = rng.standard_normal(f0.size)
+    up = fdb.Upwind(v, L, n, arith="fma")
+    up.f = f0
+    up.advect(steps, dt)
+    lam = up.f - target
+    up.f = f0
+    g0, gv = up.adjoint(steps, dt, lam, checkpoint_every=20)
+    up.close()
+    h = 1e-6
+    for k in range(4):
+        d = rng.standard_normal(f0.size)
+        fd = _fd_diff(_forward(fdb, v, L, n, f0 + h * d, steps, dt),
+                      _forward(fdb, v, L, n, f0 - h * d, steps, dt), target, h)
+        assert float(g0 @ d) == pytest.approx(fd, rel=FD_TOL)
+    for j in range(3):
+        vp, vm = v.copy(), v.copy()
+        vp[j] += h
+        vm[j] -= h
+        fd = _fd_diff(_forward(fdb, vp, L, n, f0, steps, dt),
+                      _forward(fdb, vm, L, n, f0, steps, dt), target, h)
+        assert gv[j] == pytest.approx(fd, rel=FD_TOL)
+
+
+def test_adjoint_device_buffers(fdb):
+    import torch
+    n, L, v = (16, 16, 16), (1.0, 1.0, 1.0), (0.3, -0.6, 0.9)
+    up = fdb.Upwind(v, L, n)
+    x = torch.rand(4096, dtype=torch.float64, device="cuda")
+    lam = torch.rand(4096, dtype=torch.float64, device="cuda")
+    up.set_field(x)
+    g_dev, gv_dev = up.adjoint(12, 0.02, lam)
+    up.set_field(x)
+    g_host, gv_host = up.adjoint(12, 0.02, lam.cpu().numpy())
+    assert np.array_equal(g_dev.cpu().numpy(), g_host)
+    assert np.array_equal(gv_dev, gv_host)
+    up.close()

@@ -1,0 +1,205 @@
+"""Parity of the CUDA path (through the C-ABI) with the oracle and the
+reference's golden vectors.  Bar: EXACT arithmetic is bit-identical; the FMA
+and block-fixed-point arithmetics are within 1e-13 relative max-norm after N
+steps, checksums within 1e-12 relative."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden, rel_maxnorm
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-13
+SUM_TOL = 1e-12
+ARITHS = ["exact", "fma", "fixed", "auto"]
+FIELD_CASES = golden_files("g*.npz")
+
+
+def run(fdb, n, v, L, f0, steps, dt, arith="auto", depth=0):
+    up = fdb.Upwind(v, L, n, arith="auto")
+    try:
+        up.set_arith(arith, depth)
+    except fdb.FdbError:
+        up.close()
+        raise
+    up.f = f0
+    up.advect(steps, dt)
+    out = up.f
+    cs, sd = up.checksum(), up.std()
+    used = up.arith_used
+    up.close()
+    return out, cs, sd, used
+
+
+def fixed_or_skip(fdb, arith, fn):
+    try:
+        return fn()
+    except fdb.FdbError as e:
+        if arith == "fixed" and e.code == 4:
+            pytest.skip("fixed-point kernel does not serve this geometry: " + str(e))
+        raise
+
+
+@pytest.mark.parametrize("arith", ARITHS)
+@pytest.mark.parametrize("path", FIELD_CASES, ids=lambda p: p.split("/")[-1][:-4])
+def test_golden_fields(fdb, path, arith):
+    g = load_golden(path)
+    out, cs, sd, used = fixed_or_skip(fdb, arith, lambda: run(
+        fdb, g["n"], g["v"], g["L"], g["f0"], int(g["steps"]), float(g["dt"]), arith))
+    if used == "exact":
+        assert np.array_equal(out, g["fT"]), rel_maxnorm(out, g["fT"])
+    else:
+        assert rel_maxnorm(out, g["fT"]) <= FIELD_TOL
+    assert cs == pytest.approx(float(g["checksum"]), rel=SUM_TOL, abs=1e-300)
+    assert sd == pytest.approx(float(g["std"]), rel=SUM_TOL)
+
+
+@pytest.mark.parametrize("arith", ARITHS)
+def test_reference_driver_default_128(fdb, arith):
+    """The reference driver's configuration (upwind.cxx:174-199): the
+    constructor's corner field, v = 1, courant 0.1, 128^3 x 10 steps."""
+    g = load_golden("driver_128cube_10")
+    up = fdb.Upwind([1.0] * 3, [1.0] * 3, [128] * 3)
+    fixed_or_skip(fdb, arith, lambda: up.set_arith(arith))
+    fixed_or_skip(fdb, arith, lambda: up.advect(int(g["steps"]), float(g["dt"])))
+    f = up.f
+    if up.arith_used == "exact":
+        assert np.array_equal(f[g["idx"]], g["values"])
+    else:
+        assert np.max(np.abs(f[g["idx"]] - g["values"])) <= FIELD_TOL * np.max(np.abs(f))
+    assert up.checksum() == pytest.approx(float(g["checksum"]), rel=SUM_TOL)
+    assert up.std() == pytest.approx(float(g["std"]), rel=SUM_TOL)
+    assert np.count_nonzero(f) == int(g["nonzero"])
+    up.close()
+
+
+@pytest.mark.parametrize("arith", ARITHS)
+@pytest.mark.parametrize("v", [
+    (1.0, 1.0, 1.0), (1.0, -0.7, 0.3), (-1.0, 0.7, -0.3), (-0.2, -0.9, -0.6),
+    (0.5, 0.0, -0.5), (0.0, 0.0, 0.0), (0.3, 0.3, -1.0), (-1.0, 1.0, 1.0)])
+def test_sign_combinations_vs_oracle(fdb, port, v, arith):
+    n = (19, 23, 37)
+    L = (1.0, 1.3, 0.7)
+    rng = np.random.default_rng(11)
+    f0 = rng.random(int(np.prod(n)))
+    dt = 0.33 * min(Lj / nj for Lj, nj in zip(L, n))
+    steps = 23
+    ref = port.advect(n, v, L, f0, steps, dt)
+    out, cs, sd, used = fixed_or_skip(fdb, arith, lambda: run(fdb, n, v, L, f0, steps, dt, arith))
+    if used == "exact":
+        assert np.array_equal(out, ref)
+    else:
+        assert rel_maxnorm(out, ref) <= FIELD_TOL
+    assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL)
+
+
+@pytest.mark.parametrize("arith", ARITHS)
+@pytest.mark.parametrize("n", [(1,), (2,), (1, 1, 1), (2, 2, 2), (3, 5, 7), (1, 1, 300),
+                               (300, 1, 1), (1, 300, 1), (31, 1, 33), (7, 64), (129, 3),
+                               (13, 17, 257), (2, 3, 4, 5), (2, 1, 3, 1, 2)])
+def test_edge_shapes_vs_oracle(fdb, port, n, arith):
+    nd = len(n)
+    v = [(-1.0) ** j * (0.3 + 0.2 * j) for j in range(nd)]
+    L = [1.0] * nd
+    rng = np.random.default_rng(sum(n))
+    f0 = rng.standard_normal(int(np.prod(n)))
+    dt = 0.4 * min(Lj / nj for Lj, nj in zip(L, n))
+    ref = port.advect(n, v, L, f0, 9, dt)
+    out, cs, _, used = fixed_or_skip(fdb, arith, lambda: run(fdb, n, v, L, f0, 9, dt, arith))
+    if used == "exact":
+        assert np.array_equal(out, ref)
+    else:
+        assert rel_maxnorm(out, ref) <= FIELD_TOL
+    assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL, abs=1e-12)
+
+
+@pytest.mark.parametrize("steps", [0, 1, 2, 3, 7, 8, 9, 31])
+def test_step_counts_fixed_blocking(fdb, port, steps):
+    """Step counts that are not multiples of the temporal block depth."""
+    n = (40, 36, 70)
+    v = (1.0, -0.7, 0.3)
+    L = (1.0, 1.0, 1.0)
+    f0 = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.2, 0.01, 99)
+    dt = 0.5 / 70
+    ref = port.advect(n, v, L, f0, steps, dt)
+    out, cs, _, _ = run(fdb, n, v, L, f0, steps, dt, "auto")
+    assert rel_maxnorm(out, ref) <= FIELD_TOL
+    assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL)
+
+
+def test_sphere_init_bit_exact(fdb, port):
+    g = load_golden("synth_sphere_16x12x10")
+    n = [int(x) for x in g["n"]]
+    up = fdb.Upwind([1.0] * 3, [1.0] * 3, n)
+    up.init_sphere((0.5, 0.5, 0.5), 0.2, 0.01, int(g["seed"]))
+    assert np.array_equal(up.f, g["f"])
+    up.close()
+
+
+def test_c1_config_sphere_128(fdb, port):
+    """128^3, v = (1,1,1), dt = 0.5 min dx/|v|, 10 steps, sphere r = 0.2."""
+    n = (128, 128, 128)
+    L = (1.0, 1.0, 1.0)
+    v = (1.0, 1.0, 1.0)
+    f0 = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.2, 0.0, 0)
+    dt = 0.5 / 128
+    ref = port.advect(n, v, L, f0, 10, dt)
+    for arith in ("exact", "auto"):
+        out, cs, _, used = run(fdb, n, v, L, f0, 10, dt, arith)
+        if used == "exact":
+            assert np.array_equal(out, ref)
+        assert rel_maxnorm(out, ref) <= FIELD_TOL
+        assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL)
+
+
+def test_c2_full_size_properties(fdb):
+    """512^3 x 100 (the roofline workload) is too large for the serial oracle;
+    check size-independent properties: the periodic upwind step conserves
+    sum(f), the max-norm cannot grow when sum_j a_j <= 1, the EXACT and
+    production arithmetics agree to 1e-13, and two runs are bit-identical."""
+    n = (512, 512, 512)
+    v = (1.0, -0.7, 0.3)
+    L = (1.0, 1.0, 1.0)
+    dt = 0.5 / 512
+    up = fdb.Upwind(v, L, n)
+    up.init_sphere((0.5, 0.5, 0.5), 0.2, 0.01, 20261203)
+    s0 = up.checksum()
+    f0max = float(np.max(up.f))
+    up.advect(100, dt)
+    a = up.f
+    s1 = up.checksum()
+    assert s1 == pytest.approx(s0, rel=1e-12)
+    assert float(np.max(np.abs(a))) <= f0max * (1 + 1e-14)
+    up.init_sphere((0.5, 0.5, 0.5), 0.2, 0.01, 20261203)
+    up.advect(100, dt)
+    assert np.array_equal(up.f, a)
+    up.set_arith("exact")
+    up.init_sphere((0.5, 0.5, 0.5), 0.2, 0.01, 20261203)
+    up.advect(100, dt)
+    assert rel_maxnorm(a, up.f) <= FIELD_TOL
+    up.close()
+
+
+def test_device_pointer_roundtrip(fdb):
+    import torch
+    n = (8, 9, 10)
+    up = fdb.Upwind((0.2, -0.3, 0.4), (1.0, 1.0, 1.0), n)
+    t = torch.rand(720, dtype=torch.float64, device="cuda")
+    up.set_field(t)
+    out = torch.empty_like(t)
+    up.get_field(out)
+    assert torch.equal(out, t)
+    up.close()
+
+
+def test_errors_are_loud(fdb):
+    up = fdb.Upwind((1.0,), (1.0,), (8,))
+    with pytest.raises(fdb.FdbError):
+        up.advect(-1, 0.1)
+    with pytest.raises(fdb.FdbError):
+        up.advect(1, float("nan"))
+    with pytest.raises(ValueError):
+        up.f = np.zeros(7)
+    up.close()
