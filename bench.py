@@ -55,6 +55,15 @@ BYTES_PER_CELL_UPDATE = 16.0  # read f, write f (FP64)
 WORKLOAD = "upwind3d_f64_512cube_100steps"
 
 
+def configure(n_axis: int) -> None:
+    """Cube size (512 for the benchmark; smaller cubes only for profiling)."""
+    global N_AXIS, SHAPE, DT, WORKLOAD
+    N_AXIS = n_axis
+    SHAPE = (n_axis, n_axis, n_axis)
+    DT = 0.5 / n_axis
+    WORKLOAD = f"upwind3d_f64_{n_axis}cube_100steps"
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -203,8 +212,12 @@ def main() -> None:
     ap.add_argument("--depth", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--n", type=int, default=512, help="cube size (profiling only)")
+    ap.add_argument("--tz", type=int, default=0, help="fixed kernel z-tile override")
+    ap.add_argument("--shape", type=int, default=-1, help="fixed kernel CTA shape (0..2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    configure(args.n)
 
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -222,6 +235,10 @@ def main() -> None:
     from fidibench_gb300._capi import lib
 
     up = fdb.Upwind(VELOCITY, LENGTHS, SHAPE, arith=args.arith, depth=args.depth)
+    if args.tz:
+        up.set_tile_z(args.tz)
+    if args.shape >= 0:
+        up.set_shape(args.shape)
     stream = torch.cuda.Stream()
     up.set_stream(stream)
     up.init_sphere(CENTER, RADIUS, NOISE, SEED)

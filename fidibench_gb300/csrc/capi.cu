@@ -25,8 +25,10 @@ struct fdb_upwind {
   double* dscal = nullptr;    // device scalars [8]
   double* dpart = nullptr;    // adjoint per-CTA coefficient partials [3 * adjoint_blocks()]
   double* hscal = nullptr;    // pinned host scalars [8]
-  double* scratch = nullptr;  // kernel scratch for the fixed-point path
+  double* scratch = nullptr;  // fixed-point path: max|f| slots + error word
   size_t scratch_bytes = 0;
+  int scale_slot = -1;        // scratch slot holding max|f| of the current field (-1: unknown)
+  fdb::FixedTuning tune;      // fixed kernel launch shape (depth mirrors `depth`)
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   int device = 0;
@@ -131,8 +133,18 @@ int check_handle(fdb_upwind* h) {
   return FDB_OK;
 }
 
+// Synchronise the handle's stream and report the device error word that the
+// fixed-point kernels set when they meet a non-finite input.
 int sync(fdb_upwind* h) {
   FDB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  int* err = fixed_error_word(h->scratch);
+  int herr = 0;
+  FDB_CUDA_TRY(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    FDB_CUDA_TRY(cudaMemset(err, 0, sizeof(int)));
+    return fail(FDB_ERR_NONFINITE,
+                "the field holds NaN or Inf values (the fixed-point kernel needs finite input)");
+  }
   return FDB_OK;
 }
 
@@ -164,8 +176,8 @@ int resolve_arith(fdb_upwind* h, const Coeffs3& c) {
   if (g.ndims > 3) return FDB_ARITH_EXACT;  // generic kernel
   if (h->arith == FDB_ARITH_EXACT || h->arith == FDB_ARITH_FMA) return h->arith;
   const bool ok = fixed_supported(g, c, h->depth) == FDB_OK;
-  if (h->arith == FDB_ARITH_FIXED && !ok) return -1;
-  return ok ? FDB_ARITH_FIXED : FDB_ARITH_FMA;
+  if (h->arith == FDB_ARITH_FIXED) return ok ? FDB_ARITH_FIXED : -1;
+  return (ok && fixed_preferred(g)) ? FDB_ARITH_FIXED : FDB_ARITH_FMA;
 }
 
 // Advance the handle's field by `steps` steps with the given arithmetic.
@@ -179,9 +191,14 @@ int advance(fdb_upwind* h, int steps, double dt, int arith) {
     return FDB_OK;
   }
   const Coeffs3 c = coeffs3(g, dt);
-  if (arith == FDB_ARITH_FIXED)
-    return launch_advect_fixed(g, c, steps, h->depth, h->buf, &h->cur, h->scratch,
-                               h->scratch_bytes, h->stream);
+  if (arith == FDB_ARITH_FIXED) {
+    h->tune.depth = h->depth;
+    const int rc = launch_advect_fixed_ex(g, c, steps, h->tune, h->buf, &h->cur, h->scratch,
+                                          h->scratch_bytes, &h->scale_slot, h->stream);
+    if (rc) h->scale_slot = -1;
+    return rc;
+  }
+  h->scale_slot = -1;
   for (int s = 0; s < steps; ++s) {
     FDB_TRY(launch_step_f64(g, c, arith, h->buf[h->cur], h->buf[h->cur ^ 1], h->stream));
     h->cur ^= 1;
@@ -218,11 +235,14 @@ int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
   h->stream = h->own;
   if ((rc = dalloc(&h->buf[0], g.ntot)) || (rc = dalloc(&h->buf[1], g.ntot)) ||
       (rc = dalloc(&h->part, reduce_partials(g.ntot))) || (rc = dalloc(&h->dscal, 8)) ||
-      (rc = dalloc(&h->dpart, 3 * (size_t)adjoint_blocks()))) {
+      (rc = dalloc(&h->dpart, 3 * (size_t)adjoint_blocks())) ||
+      (rc = dalloc(&h->scratch, (fixed_scratch_bytes() + 7) / 8))) {
     fdb_upwind_destroy(h);
     return rc;
   }
-  e = cudaMallocHost((void**)&h->hscal, 8 * sizeof(double));
+  h->scratch_bytes = (fixed_scratch_bytes() + 7) / 8 * 8;
+  e = cudaMemsetAsync(h->scratch, 0, h->scratch_bytes, h->stream);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&h->hscal, 8 * sizeof(double));
   if (e != cudaSuccess) {
     fdb_upwind_destroy(h);
     return cuda_fail(e, "cudaMallocHost");
@@ -257,6 +277,7 @@ int fdb_upwind_destroy(fdb_upwind* h) {
 int fdb_upwind_set_field(fdb_upwind* h, const double* src, int is_device) {
   FDB_TRY(check_handle(h));
   if (!src) return fail(FDB_ERR_INVALID, "null source field");
+  h->scale_slot = -1;
   FDB_CUDA_TRY(cudaMemcpyAsync(h->buf[h->cur], src, h->g.ntot * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                h->stream));
@@ -276,6 +297,7 @@ int fdb_upwind_field_ptr(fdb_upwind* h, double** out) {
   FDB_TRY(check_handle(h));
   if (!out) return fail(FDB_ERR_INVALID, "null output pointer");
   *out = h->buf[h->cur];
+  h->scale_slot = -1;  // the caller may write through the pointer
   return FDB_OK;
 }
 
@@ -336,6 +358,21 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth) {
   return FDB_OK;
 }
 
+int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value) {
+  FDB_TRY(check_handle(h));
+  if (key == FDB_TUNE_TILE_Z) {
+    if (value < 0) return fail(FDB_ERR_INVALID, "tile_z must be >= 0");
+    h->tune.tz = value;
+    return FDB_OK;
+  }
+  if (key == FDB_TUNE_SHAPE) {
+    if (value < -1 || value > 2) return fail(FDB_ERR_INVALID, "shape must be in [-1, 2]");
+    h->tune.shape = value;
+    return FDB_OK;
+  }
+  return fail(FDB_ERR_INVALID, "unknown tuning key");
+}
+
 int fdb_upwind_info(fdb_upwind* h, uint64_t* ntot, int* arith_used) {
   FDB_TRY(check_handle(h));
   if (ntot) *ntot = h->g.ntot;
@@ -347,6 +384,7 @@ int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius, d
                            uint64_t seed) {
   FDB_TRY(check_handle(h));
   if (!center) return fail(FDB_ERR_INVALID, "null centre");
+  h->scale_slot = -1;
   FDB_TRY(launch_sphere_noise(h->g, center, radius, noise_amp, seed, h->buf[h->cur], h->stream));
   return sync(h);
 }

@@ -78,9 +78,25 @@ int launch_step_generic(const Geom& g, double dt, const double* in, double* out,
 // `depth`).  Returns FDB_ERR_UNSUPPORTED when the geometry or coefficients
 // are outside what it serves (the caller then uses the FP64 kernel).
 int fixed_supported(const Geom& g, const Coeffs3& c, int depth);
+bool fixed_preferred(const Geom& g);
+size_t fixed_scratch_bytes();
+// Device error word inside the fixed kernel's scratch (non-zero: non-finite input).
+int* fixed_error_word(double* d_scratch);
+// Launch-shape knobs of the fixed kernel (0 / -1 = automatic).
+struct FixedTuning {
+  int depth = 0;   // temporal depth K (steps per launch), 1..4
+  int shape = -1;  // rows x warps per CTA: 0 = 8x8, 1 = 4x16, 2 = 4x32
+  int tz = 0;      // output planes per CTA along z
+};
+
 int launch_advect_fixed(const Geom& g, const Coeffs3& c, int steps, int depth,
                         double** buf, int* cur, double* d_scratch, size_t scratch_bytes,
                         cudaStream_t s);
+// As above; *scale_slot (in/out, may be null) names the scratch slot that
+// holds max|f| of the current field (-1: unknown, a pre-pass measures it).
+int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const FixedTuning& tune,
+                           double** buf, int* cur, double* d_scratch, size_t scratch_bytes,
+                           int* scale_slot, cudaStream_t s);
 
 // Deterministic reductions.  `part` holds at least reduce_partials(n) doubles.
 uint32_t reduce_partials(uint64_t n);

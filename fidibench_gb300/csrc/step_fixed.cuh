@@ -1,0 +1,284 @@
+// step_fixed.cuh -- the temporally blocked block-fixed-point upwind kernel
+// (template), included by the per-shape translation units step_fixed_*.cu.
+// The algorithm, precision argument and scale protocol are described in
+// step_fixed.cu.
+#pragma once
+
+#include "fdb_internal.h"
+#include "fixed_point.cuh"
+
+namespace fdb {
+namespace fx {
+
+struct ScaleSlot {
+  unsigned long long m;  // kind 0: FP64 bits of max|f|; kind 1: OR of |F| at scale s
+  int s;
+  int kind;
+};
+
+struct FixedArgs {
+  int nz, ny, nx;
+  int fz, fy, fx;  // 1: physical axis reversed relative to the logical one
+  int tx, ty, tz;
+  int tiles_x, tiles_y, tiles_z;
+  QCoeff qz, qy, qx;
+  int guard;
+  const ScaleSlot* slot_in;
+  ScaleSlot* slot_out;
+  ScaleSlot* slot_reset;
+  int* err;
+};
+
+__device__ __forceinline__ int wrap_mod(int i, int n) {
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ int64_t mad_s(int32_t a, int32_t b, int64_t c) {
+  int64_t d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ uint64_t mad_u(uint32_t a, uint32_t b, uint64_t c) {
+  uint64_t d;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+
+// One level for one cell: F' = F + 4 * sum_j A_j D_j / 2^64 with D_j =
+// F_up_j - F.  The a1*d1 products accumulate exactly; the two families of
+// 32x32 partial products (a0*d1 signed, a1*d0 unsigned) are each summed
+// exactly in 64 bits from 2^31 and their high words taken, i.e. rounded to
+// nearest: unbiased, and exactly zero when every D_j is zero.
+__device__ __forceinline__ int64_t update(int64_t c, int64_t zb, int64_t up, int64_t left,
+                                          const FixedArgs& a) {
+  const int64_t Dz = zb - c, Dy = up - c, Dx = left - c;
+  const int32_t z1 = (int32_t)(Dz >> 32), y1 = (int32_t)(Dy >> 32), x1 = (int32_t)(Dx >> 32);
+  const uint32_t z0 = (uint32_t)Dz, y0 = (uint32_t)Dy, x0 = (uint32_t)Dx;
+  int64_t acc = mad_s(a.qz.a1, z1, 0);
+  acc = mad_s(a.qy.a1, y1, acc);
+  acc = mad_s(a.qx.a1, x1, acc);
+  int64_t h = mad_s(a.qz.a0, z1, 0x80000000ll);
+  h = mad_s(a.qy.a0, y1, h);
+  h = mad_s(a.qx.a0, x1, h);
+  uint64_t v = mad_u((uint32_t)a.qz.a1, z0, 0x80000000ull);
+  v = mad_u((uint32_t)a.qy.a1, y0, v);
+  v = mad_u((uint32_t)a.qx.a1, x0, v);
+  acc += (h >> 32) + (int64_t)(v >> 32);
+  return c + acc * 4;
+}
+
+// R rows per thread, W warps per CTA (stacked in y): region 32 x (R*W).
+template <int K, int R, int W, int MINB, bool IN_F64, bool OUT_F64>
+__global__ void __launch_bounds__(32 * W, MINB)
+k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
+  constexpr int kThreads = 32 * W;
+  // prefetch buffers [2][R][kThreads] in dynamic shared memory (64 KB for R4W32)
+  extern __shared__ __align__(16) int64_t s_dyn[];
+  int64_t(*s_pre)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn);
+  __shared__ int64_t s_row[2][W][32];
+  __shared__ unsigned long long s_or[W];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  int bid = blockIdx.x;
+  const int tile_x = bid % a.tiles_x;
+  bid /= a.tiles_x;
+  const int tile_y = bid % a.tiles_y;
+  const int tile_z = bid / a.tiles_y;
+
+  // ---- scale of this launch ----------------------------------------------
+  const unsigned long long M = a.slot_in->m;
+  const int kind = a.slot_in->kind;
+  const int s_in = a.slot_in->s;
+  const int T = 58 - a.guard;  // highest bit allowed for |F| at the input
+  int s = 0, d = 0;
+  if (kind == 0) {
+    if (M >= 0x7FF0000000000000ull) {
+      if (tid == 0) atomicOr(a.err, 1);  // NaN/Inf in the input field
+    } else if (M != 0ull) {
+      s = T + 1023 - (int)(M >> 52);  // max|f| < 2^(E-1022)  ->  |F| < 2^(T+1)
+    }
+  } else if (M != 0ull) {
+    d = T - (63 - __clzll((long long)M));
+    d = d > 62 ? 62 : (d < -62 ? -62 : d);
+    s = s_in + d;
+  } else {
+    s = s_in;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    a.slot_reset->m = 0ull;
+    a.slot_reset->kind = 1;
+    a.slot_out->s = s;
+    a.slot_out->kind = 1;
+  }
+
+  const int X0 = tile_x * a.tx;
+  const int Y0 = tile_y * a.ty;
+  const int Z0 = tile_z * a.tz;
+
+  const int lx = wrap_mod(X0 - K + lane, a.nx);
+  const int px = a.fx ? a.nx - 1 - lx : lx;
+  const bool out_x = (lane >= K) && (X0 + lane - K < a.nx);
+
+  // offset (py * nx + px) of row r; rows that do not wrap form an arithmetic
+  // progression, so only the first offset and the step stay in registers
+  const int ly0 = Y0 - K + warp * R;
+  const bool rows_linear = (ly0 >= 0) && (ly0 + R - 1 < a.ny);
+  const int rstep = a.fy ? -a.nx : a.nx;
+  const int roff0 = (a.fy ? a.ny - 1 - wrap_mod(ly0, a.ny) : wrap_mod(ly0, a.ny)) * a.nx + px;
+  auto row_off = [&](int r) -> int {
+    if (rows_linear) return roff0 + r * rstep;
+    const int ly = wrap_mod(ly0 + r, a.ny);
+    return (a.fy ? a.ny - 1 - ly : ly) * a.nx + px;
+  };
+  const int64_t plane_sz = (int64_t)a.ny * a.nx;
+  const int nplanes = a.tz + K;
+  auto plane_off = [&](int p) -> int64_t {
+    const int lz = wrap_mod(Z0 - K + p, a.nz);
+    return (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
+  };
+
+  int64_t hist[K][R];
+  int64_t cur[R];
+#pragma unroll
+  for (int t = 0; t < K; ++t)
+#pragma unroll
+    for (int r = 0; r < R; ++r) hist[t][r] = 0;
+
+  {
+    const int64_t po = plane_off(0);
+#pragma unroll
+    for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], in + po + row_off(r));
+    cp_async_commit();
+  }
+
+  unsigned long long my_or = 0ull;
+  int parity = 0;
+  for (int p = 0; p < nplanes; ++p) {
+    if (p + 1 < nplanes) {
+      const int64_t po = plane_off(p + 1);
+#pragma unroll
+      for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], in + po + row_off(r));
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int64_t raw = s_pre[p & 1][r][tid];
+      if (IN_F64) {
+        cur[r] = to_fixed(__longlong_as_double(raw), s);
+      } else {
+        cur[r] = d >= 0 ? (raw << d) : (raw >> (-d));
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < K; ++t) {
+      s_row[parity][warp][lane] = cur[R - 1];
+      __syncthreads();
+      const int64_t up0 = (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0];
+      parity ^= 1;
+      int64_t left[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
+#pragma unroll
+      for (int r = R - 1; r >= 0; --r) {
+        const int64_t c = cur[r];
+        const int64_t lf = (lane == 0) ? c : left[r];
+        const int64_t upv = (r > 0) ? cur[r - 1] : up0;
+        const int64_t nv = update(c, hist[t][r], upv, lf, a);
+        hist[t][r] = c;
+        cur[r] = nv;
+      }
+    }
+    if (p >= K && Z0 + p - K < a.nz) {
+      const int64_t po = plane_off(p);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int ry = warp * R + r;
+        if (out_x && ry >= K && Y0 + ry - K < a.ny) {
+          const int64_t v = cur[r];
+          my_or |= (unsigned long long)(v ^ (v >> 63));
+          if (OUT_F64)
+            out[po + row_off(r)] = __double_as_longlong(to_double(v, s));
+          else
+            out[po + row_off(r)] = v;
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();
+
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) my_or |= __shfl_xor_sync(0xffffffffu, my_or, o);
+  if (lane == 0) s_or[warp] = my_or;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long m = 0ull;
+#pragma unroll
+    for (int w = 0; w < W; ++w) m |= s_or[w];
+    if (m) atomicOr(&a.slot_out->m, m);
+  }
+}
+
+// Kernel shapes compiled into the library (rows per thread x warps per CTA).
+enum Shape { kR8W8 = 0, kR4W16 = 1, kR4W32 = 2, kNumShapes = 3 };
+constexpr int shape_rows(int sh) { return sh == kR8W8 ? 8 : 4; }
+constexpr int shape_warps(int sh) { return sh == kR8W8 ? 8 : (sh == kR4W16 ? 16 : 32); }
+
+template <int K, int R, int W, int MINB, bool IN, bool OUT>
+void launch_k(unsigned blocks, const int64_t* in, int64_t* out, const FixedArgs& a,
+              cudaStream_t st) {
+  constexpr int smem = 2 * R * 32 * W * (int)sizeof(int64_t);
+  static bool configured = false;  // per instantiation; benign race (idempotent)
+  if (!configured) {
+    cudaFuncSetAttribute(k_advect_fixed<K, R, W, MINB, IN, OUT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    configured = true;
+  }
+  k_advect_fixed<K, R, W, MINB, IN, OUT><<<blocks, 32 * W, smem, st>>>(in, out, a);
+}
+
+template <int K, int R, int W, int MINB>
+void launch_io(bool in_f64, bool out_f64, unsigned blocks, const int64_t* in, int64_t* out,
+               const FixedArgs& a, cudaStream_t st) {
+  if (in_f64 && out_f64) launch_k<K, R, W, MINB, true, true>(blocks, in, out, a, st);
+  else if (in_f64) launch_k<K, R, W, MINB, true, false>(blocks, in, out, a, st);
+  else if (out_f64) launch_k<K, R, W, MINB, false, true>(blocks, in, out, a, st);
+  else launch_k<K, R, W, MINB, false, false>(blocks, in, out, a, st);
+}
+
+template <int R, int W, int MINB>
+void launch_shape(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+                  int64_t* out, const FixedArgs& a, cudaStream_t st) {
+  switch (K) {
+    case 1: launch_io<1, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 2: launch_io<2, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 3: launch_io<3, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    default: launch_io<4, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+  }
+}
+
+// defined in step_fixed_<shape>.cu
+void launch_r8w8(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+                 int64_t* out, const FixedArgs& a, cudaStream_t st);
+void launch_r4w16(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+                  int64_t* out, const FixedArgs& a, cudaStream_t st);
+void launch_r4w32(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+                  int64_t* out, const FixedArgs& a, cudaStream_t st);
+
+}  // namespace fx
+}  // namespace fdb

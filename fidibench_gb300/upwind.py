@@ -76,6 +76,15 @@ class Upwind:
         code = _capi.ARITH_NAMES[arith] if isinstance(arith, str) else int(arith)
         check(lib.fdb_upwind_set_arith(self._h, code, int(depth)))
 
+    def set_tile_z(self, tile_z: int) -> None:
+        """Output planes per CTA of the fixed-point kernel (0 = automatic)."""
+        check(lib.fdb_upwind_set_tuning(self._h, 1, int(tile_z)))
+
+    def set_shape(self, shape: int) -> None:
+        """Fixed-point kernel CTA shape: 0 = 8 rows x 8 warps, 1 = 4 x 16,
+        2 = 4 x 32, -1 = automatic."""
+        check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
+
     def set_stream(self, stream) -> None:
         """Enqueue on a CUDA stream (a torch.cuda.Stream, a raw handle or None)."""
         raw = getattr(stream, "cuda_stream", stream)

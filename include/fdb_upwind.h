@@ -100,6 +100,14 @@ int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream);
  * the FIXED kernel (0 = autotuned/default). */
 int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
 
+/* Launch-shape tuning of the FIXED kernel (the autotuner's knobs).
+ *  FDB_TUNE_TILE_Z : output planes per CTA along the slowest axis (0 = auto).
+ *  FDB_TUNE_SHAPE  : rows per thread x warps per CTA: 0 = 8x8, 1 = 4x16,
+ *                    2 = 4x32 (-1 = auto). */
+#define FDB_TUNE_TILE_Z 1
+#define FDB_TUNE_SHAPE 2
+int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value);
+
 /* Number of cells, and the arithmetic the last advect actually used. */
 int fdb_upwind_info(fdb_upwind* h, uint64_t* ntot, int* arith_used);
 
