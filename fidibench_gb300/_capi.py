@@ -51,6 +51,7 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_set_arith": (_int, [_vp, _int, _int]),
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),
+    "fdb_checksum_noalloc": (_int, [_vp, ctypes.c_uint64, _vp, _vp]),
     "fdb_upwind_init_sphere": (_int, [_vp, _vp, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_uint64]),
     "fdb_upwind_adjoint": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _vp, _int, _int]),

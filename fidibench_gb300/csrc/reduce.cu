@@ -114,3 +114,70 @@ int launch_std(const double* f, uint64_t n, double* part, double* d_tmp, double*
 }
 
 }  // namespace fdb
+
+// ---------------------------------------------------------------------------
+// fdb_checksum_noalloc: the checksum reduction for callers that cannot
+// allocate device memory.
+//
+// Some callers must not allocate GPU memory while they run: code that runs
+// inside a memory pool or arena that owns all device memory, real-time or
+// embedded hosts that forbid allocation after start-up, and callbacks that
+// run where cudaMalloc would synchronise the device or fail.  This entry point
+// runs the same two kernels as fdb_upwind_checksum (same chunking, so the same
+// result bit for bit), but keeps the per-CTA partial sums in the file-scope
+// array below instead of memory that a handle allocated.
+//
+// Limits and sharing: the array holds kNoAllocPartials (2048) doubles, 16 KB,
+// which every GPU that loads this library keeps until the process exits.  The
+// reduction never needs more than 2048 partials; fields are accepted up to
+// FDB_NOALLOC_MAX_VALUES values.  Every call writes every partial it later
+// reads, so nothing has to be cleared between calls, but all calls share the
+// one array: calls whose kernels overlap on the GPU (on different streams, or
+// from different host threads) race and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr uint32_t kNoAllocPartials = 2048;
+static_assert(kNoAllocPartials >= fdb::kMaxPartials, "scratch must hold every partial");
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_partials on the current device (looked up once
+// per device; the host-side symbol is not a device address).
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  FDB_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fdb::fail(FDB_ERR_UNSUPPORTED, "device ordinal beyond the no-allocation table");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    FDB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    g_noalloc_ptr[dev] = (double*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return FDB_OK;
+}
+
+}  // namespace
+
+extern "C" int fdb_checksum_noalloc(const double* d_field, uint64_t n, double* d_sum,
+                                    void* cuda_stream) {
+  if (!d_field || !d_sum) return fdb::fail(FDB_ERR_INVALID, "null field or result pointer");
+  if (n == 0 || n > FDB_NOALLOC_MAX_VALUES)
+    return fdb::fail(FDB_ERR_INVALID,
+                     "fdb_checksum_noalloc: n must be in [1, FDB_NOALLOC_MAX_VALUES = 2^34]");
+  const uint32_t g = fdb::reduce_partials(n);
+  if (g > kNoAllocPartials)
+    return fdb::fail(FDB_ERR_INVALID, "fdb_checksum_noalloc: field needs more partial sums "
+                                      "than the 2048-entry static scratch holds");
+  double* part = nullptr;
+  FDB_TRY(noalloc_scratch(&part));
+  return fdb::launch_sum(d_field, n, part, d_sum, (cudaStream_t)cuda_stream);
+}

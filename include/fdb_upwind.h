@@ -138,6 +138,26 @@ int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
                             const double* lam_in_dev, double* lam_out_dev,
                             double* dcoef_host);
 
+/* ---------------------------------------------------------------------------
+ * Checksum without any allocation.  No counterpart in the reference: it exists
+ * for callers that may not allocate GPU memory while they run (a memory pool
+ * or arena that owns all device memory, a host that forbids allocation after
+ * start-up, a callback where cudaMalloc would synchronise or fail).
+ *
+ * Sums n FP64 values at d_field (device memory) into *d_sum (device memory),
+ * enqueued on cuda_stream (a cudaStream_t; NULL = legacy default stream) and
+ * not synchronised.  Same kernels and chunking as fdb_upwind_checksum, so the
+ * same result.  Scratch is a 2048-double (16 KB) static device array that the
+ * library keeps on every GPU it is loaded on until the process exits; nothing
+ * in it needs clearing between calls.  Calls that overlap on the GPU share the
+ * array and race: serialise them.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * n must be in [1, FDB_NOALLOC_MAX_VALUES]; other sizes return
+ * FDB_ERR_INVALID.
+ * ------------------------------------------------------------------------- */
+#define FDB_NOALLOC_MAX_VALUES (1ull << 34)
+int fdb_checksum_noalloc(const double* d_field, uint64_t n, double* d_sum, void* cuda_stream);
+
 /* Number of kernels this library has launched in this process (all handles,
  * all threads).  A diagnostic for benchmarks; no reference counterpart. */
 uint64_t fdb_launch_count(void);
