@@ -85,7 +85,7 @@ int* fixed_error_word(double* d_scratch);
 // Launch-shape knobs of the fixed kernel (0 / -1 = automatic).
 struct FixedTuning {
   int depth = 0;   // temporal depth K (steps per launch), 1..4
-  int shape = -1;  // rows x warps per CTA: 0 = 8x8, 1 = 4x16, 2 = 4x32
+  int shape = -1;  // 0 = 8x8, 1 = 4x16 (history in registers), 2 = 8x8, 3 = 4x16 (in smem)
   int tz = 0;      // output planes per CTA along z
 };
 

@@ -30,7 +30,8 @@
 // output tile of (32-K) x (R*W-K) cells in (x, y) and marches along z over tz
 // output planes after K warm-up planes.  Lanes are consecutive x (coalesced
 // 256 B row accesses), each thread holds R consecutive y rows of one column
-// in registers (shapes R x W = 8x8, 4x16, 4x32 are compiled).  Per level: x-1 from lane-1 by SHFL, y-1 from the thread's
+// in registers (shapes R x W = 8x8 and 4x16 are compiled, each with the
+// plane history in registers or in shared memory).  Per level: x-1 from lane-1 by SHFL, y-1 from the thread's
 // previous row (row 0 from the warp above through shared memory, one
 // __syncthreads per level), z-1 from the thread's K-deep history of the
 // previous plane.  The next plane is prefetched with cp.async into shared
@@ -138,7 +139,8 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
   int64_t* pout = (int64_t*)out;
   switch (shape) {
     case fx::kR4W16: fx::launch_r4w16(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
-    case fx::kR4W32: fx::launch_r4w32(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
+    case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
+    case fx::kR4W16S: fx::launch_r4w16s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
     default: fx::launch_r8w8(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
   }
   note_launch();
@@ -192,7 +194,9 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   ScaleSlot* slots = (ScaleSlot*)d_scratch;
   int* err = fixed_error_word(d_scratch);
   const int K = tune.depth > 0 ? tune.depth : default_depth();
-  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : fx::kR8W8;
+  // default: 4 rows x 16 warps with the plane history in shared memory (the
+  // fastest measured shape at 512^3, K = 4)
+  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : fx::kR4W16S;
   int i0 = (scale_slot && *scale_slot >= 0) ? *scale_slot : -1;
   if (i0 < 0) {
     k_slots_init<<<1, 32, 0, s>>>(slots);

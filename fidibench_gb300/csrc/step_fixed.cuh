@@ -80,14 +80,24 @@ __device__ __forceinline__ int64_t update(int64_t c, int64_t zb, int64_t up, int
   return c + acc * 4;
 }
 
+// Dynamic shared memory of one CTA: plane prefetch [2][R][threads], plus the
+// K-deep plane history [K][R][threads] when HSM (history in shared memory).
+template <int K, int R, int W, bool HSM>
+constexpr int fixed_smem_bytes() {
+  return (2 + (HSM ? K : 0)) * R * 32 * W * (int)sizeof(int64_t);
+}
+
 // R rows per thread, W warps per CTA (stacked in y): region 32 x (R*W).
-template <int K, int R, int W, int MINB, bool IN_F64, bool OUT_F64>
+// HSM keeps the plane history in shared memory (each thread touches only its
+// own slots, so it needs no barrier) and frees 2*K*R registers per thread for
+// row updates in flight.
+template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64>
 __global__ void __launch_bounds__(32 * W, MINB)
 k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
   constexpr int kThreads = 32 * W;
-  // prefetch buffers [2][R][kThreads] in dynamic shared memory (64 KB for R4W32)
   extern __shared__ __align__(16) int64_t s_dyn[];
   int64_t(*s_pre)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn);
+  int64_t(*s_hist)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn + 2 * R * kThreads);
   __shared__ int64_t s_row[2][W][32];
   __shared__ unsigned long long s_or[W];
 
@@ -147,78 +157,113 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
   };
   const int64_t plane_sz = (int64_t)a.ny * a.nx;
   const int nplanes = a.tz + K;
-  auto plane_off = [&](int p) -> int64_t {
-    const int lz = wrap_mod(Z0 - K + p, a.nz);
-    return (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
+  auto plane_ptr = [&](const int64_t* base, int lz) {
+    return base + (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
   };
+  // rows this thread writes: bit r set when row r lies in the tile and the grid
+  unsigned row_mask = 0u;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int ry = warp * R + r;
+    if (out_x && ry >= K && Y0 + ry - K < a.ny) row_mask |= 1u << r;
+  }
 
-  int64_t hist[K][R];
+  int64_t hist[HSM ? 1 : K][R];
   int64_t cur[R];
 #pragma unroll
-  for (int t = 0; t < K; ++t)
+  for (int t = 0; t < (HSM ? 1 : K); ++t)
 #pragma unroll
     for (int r = 0; r < R; ++r) hist[t][r] = 0;
-
-  {
-    const int64_t po = plane_off(0);
+  if (HSM) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], in + po + row_off(r));
+    for (int t = 0; t < K; ++t)
+#pragma unroll
+      for (int r = 0; r < R; ++r) s_hist[t][r][tid] = 0;
+  }
+
+  // logical z of the plane being computed; advanced by one per iteration
+  int lz = wrap_mod(Z0 - K, a.nz);
+  {
+    const int64_t* src = plane_ptr(in, lz);
+#pragma unroll
+    for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], src + row_off(r));
     cp_async_commit();
   }
 
   unsigned long long my_or = 0ull;
   int parity = 0;
   for (int p = 0; p < nplanes; ++p) {
+    const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
     if (p + 1 < nplanes) {
-      const int64_t po = plane_off(p + 1);
+      const int64_t* src = plane_ptr(in, lz_next);
 #pragma unroll
-      for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], in + po + row_off(r));
+      for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], src + row_off(r));
     }
     cp_async_commit();
     cp_async_wait<1>();
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int64_t raw = s_pre[p & 1][r][tid];
-      if (IN_F64) {
-        cur[r] = to_fixed(__longlong_as_double(raw), s);
-      } else {
-        cur[r] = d >= 0 ? (raw << d) : (raw >> (-d));
-      }
+      if (IN_F64) cur[r] = to_fixed(__longlong_as_double(raw), s);
+      else cur[r] = raw;
+    }
+    if (!IN_F64 && d != 0) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) cur[r] = d > 0 ? (cur[r] << d) : (cur[r] >> (-d));
     }
 #pragma unroll
     for (int t = 0; t < K; ++t) {
+      // warm-up plane p holds valid levels 0..p only: level t+1 is skipped for
+      // t >= p (uniform across the CTA), but level t is still recorded as the
+      // history that level t+1 of the next plane reads
+      if (p < K && t >= p) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (HSM) s_hist[t][r][tid] = cur[r];
+          else hist[HSM ? 0 : t][r] = cur[r];
+        }
+        continue;
+      }
+      int64_t zb[R];
+      if (HSM) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) zb[r] = s_hist[t][r][tid];
+      }
       s_row[parity][warp][lane] = cur[R - 1];
       __syncthreads();
       const int64_t up0 = (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0];
       parity ^= 1;
+      // x-1 neighbour; lane 0 (the tile's halo column) receives its own value
       int64_t left[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
 #pragma unroll
       for (int r = R - 1; r >= 0; --r) {
         const int64_t c = cur[r];
-        const int64_t lf = (lane == 0) ? c : left[r];
         const int64_t upv = (r > 0) ? cur[r - 1] : up0;
-        const int64_t nv = update(c, hist[t][r], upv, lf, a);
-        hist[t][r] = c;
+        const int64_t nv = update(c, HSM ? zb[r] : hist[HSM ? 0 : t][r], upv, left[r], a);
+        if (HSM)
+          s_hist[t][r][tid] = c;
+        else
+          hist[HSM ? 0 : t][r] = c;
         cur[r] = nv;
       }
     }
     if (p >= K && Z0 + p - K < a.nz) {
-      const int64_t po = plane_off(p);
+      int64_t* dst = const_cast<int64_t*>(plane_ptr(out, lz));
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int ry = warp * R + r;
-        if (out_x && ry >= K && Y0 + ry - K < a.ny) {
+        if (row_mask & (1u << r)) {
           const int64_t v = cur[r];
           my_or |= (unsigned long long)(v ^ (v >> 63));
           if (OUT_F64)
-            out[po + row_off(r)] = __double_as_longlong(to_double(v, s));
+            dst[row_off(r)] = __double_as_longlong(to_double(v, s));
           else
-            out[po + row_off(r)] = v;
+            dst[row_off(r)] = v;
         }
       }
     }
+    lz = lz_next;
   }
   cp_async_wait<0>();
 
@@ -234,51 +279,54 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
   }
 }
 
-// Kernel shapes compiled into the library (rows per thread x warps per CTA).
-enum Shape { kR8W8 = 0, kR4W16 = 1, kR4W32 = 2, kNumShapes = 3 };
-constexpr int shape_rows(int sh) { return sh == kR8W8 ? 8 : 4; }
-constexpr int shape_warps(int sh) { return sh == kR8W8 ? 8 : (sh == kR4W16 ? 16 : 32); }
+// Kernel shapes compiled into the library: rows per thread x warps per CTA,
+// history in registers (reg) or shared memory (smem).
+enum Shape { kR8W8 = 0, kR4W16 = 1, kR8W8S = 2, kR4W16S = 3, kNumShapes = 4 };
+constexpr int shape_rows(int sh) { return (sh == kR8W8 || sh == kR8W8S) ? 8 : 4; }
+constexpr int shape_warps(int sh) { return (sh == kR8W8 || sh == kR8W8S) ? 8 : 16; }
 
-template <int K, int R, int W, int MINB, bool IN, bool OUT>
+template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT>
 void launch_k(unsigned blocks, const int64_t* in, int64_t* out, const FixedArgs& a,
               cudaStream_t st) {
-  constexpr int smem = 2 * R * 32 * W * (int)sizeof(int64_t);
+  constexpr int smem = fixed_smem_bytes<K, R, W, HSM>();
   static bool configured = false;  // per instantiation; benign race (idempotent)
   if (!configured) {
-    cudaFuncSetAttribute(k_advect_fixed<K, R, W, MINB, IN, OUT>,
+    cudaFuncSetAttribute(k_advect_fixed<K, R, W, HSM, MINB, IN, OUT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     configured = true;
   }
-  k_advect_fixed<K, R, W, MINB, IN, OUT><<<blocks, 32 * W, smem, st>>>(in, out, a);
+  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT><<<blocks, 32 * W, smem, st>>>(in, out, a);
 }
 
-template <int K, int R, int W, int MINB>
+template <int K, int R, int W, bool HSM, int MINB>
 void launch_io(bool in_f64, bool out_f64, unsigned blocks, const int64_t* in, int64_t* out,
                const FixedArgs& a, cudaStream_t st) {
-  if (in_f64 && out_f64) launch_k<K, R, W, MINB, true, true>(blocks, in, out, a, st);
-  else if (in_f64) launch_k<K, R, W, MINB, true, false>(blocks, in, out, a, st);
-  else if (out_f64) launch_k<K, R, W, MINB, false, true>(blocks, in, out, a, st);
-  else launch_k<K, R, W, MINB, false, false>(blocks, in, out, a, st);
+  if (in_f64 && out_f64) launch_k<K, R, W, HSM, MINB, true, true>(blocks, in, out, a, st);
+  else if (in_f64) launch_k<K, R, W, HSM, MINB, true, false>(blocks, in, out, a, st);
+  else if (out_f64) launch_k<K, R, W, HSM, MINB, false, true>(blocks, in, out, a, st);
+  else launch_k<K, R, W, HSM, MINB, false, false>(blocks, in, out, a, st);
 }
 
-template <int R, int W, int MINB>
+template <int R, int W, bool HSM, int MINB>
 void launch_shape(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
                   int64_t* out, const FixedArgs& a, cudaStream_t st) {
   switch (K) {
-    case 1: launch_io<1, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    case 2: launch_io<2, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    case 3: launch_io<3, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    default: launch_io<4, R, W, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 1: launch_io<1, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 2: launch_io<2, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 3: launch_io<3, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    default: launch_io<4, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
   }
 }
 
 // defined in step_fixed_<shape>.cu
-void launch_r8w8(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
-                 int64_t* out, const FixedArgs& a, cudaStream_t st);
-void launch_r4w16(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
-                  int64_t* out, const FixedArgs& a, cudaStream_t st);
-void launch_r4w32(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
-                  int64_t* out, const FixedArgs& a, cudaStream_t st);
+#define FDB_FX_DECLARE(NAME)                                                               \
+  void NAME(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,          \
+            int64_t* out, const FixedArgs& a, cudaStream_t st);
+FDB_FX_DECLARE(launch_r8w8)
+FDB_FX_DECLARE(launch_r4w16)
+FDB_FX_DECLARE(launch_r8w8s)
+FDB_FX_DECLARE(launch_r4w16s)
+#undef FDB_FX_DECLARE
 
 }  // namespace fx
 }  // namespace fdb

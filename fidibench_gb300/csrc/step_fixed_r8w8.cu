@@ -1,6 +1,6 @@
-// step_fixed_r8w8.cu -- instantiations of the fixed-point kernel for 8 rows per
-// thread and 8 warps per CTA (a separate translation unit so the shapes
-// compile in parallel).
+// step_fixed_r8w8.cu -- instantiations of the fixed-point kernel: 8 rows per
+// thread, 8 warps per CTA, plane history in registers (a separate
+// translation unit so that the shapes compile in parallel).
 #include "step_fixed.cuh"
 
 namespace fdb {
@@ -8,7 +8,7 @@ namespace fx {
 
 void launch_r8w8(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
                  int64_t* out, const FixedArgs& a, cudaStream_t st) {
-  launch_shape<8, 8, 2>(K, in_f64, out_f64, blocks, in, out, a, st);
+  launch_shape<8, 8, false, 2>(K, in_f64, out_f64, blocks, in, out, a, st);
 }
 
 }  // namespace fx

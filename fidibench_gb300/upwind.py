@@ -81,8 +81,9 @@ class Upwind:
         check(lib.fdb_upwind_set_tuning(self._h, 1, int(tile_z)))
 
     def set_shape(self, shape: int) -> None:
-        """Fixed-point kernel CTA shape: 0 = 8 rows x 8 warps, 1 = 4 x 16,
-        2 = 4 x 32, -1 = automatic."""
+        """Fixed-point kernel CTA shape: 0 = 8 rows x 8 warps, 1 = 4 x 16 (plane
+        history in registers), 2 = 8 x 8, 3 = 4 x 16 (history in shared
+        memory), -1 = automatic."""
         check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
 
     def set_stream(self, stream) -> None:

@@ -102,8 +102,9 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
 
 /* Launch-shape tuning of the FIXED kernel (the autotuner's knobs).
  *  FDB_TUNE_TILE_Z : output planes per CTA along the slowest axis (0 = auto).
- *  FDB_TUNE_SHAPE  : rows per thread x warps per CTA: 0 = 8x8, 1 = 4x16,
- *                    2 = 4x32 (-1 = auto). */
+ *  FDB_TUNE_SHAPE  : rows per thread x warps per CTA and where the plane
+ *                    history lives: 0 = 8x8 registers, 1 = 4x16 registers,
+ *                    2 = 8x8 shared memory, 3 = 4x16 shared memory (-1 = auto). */
 #define FDB_TUNE_TILE_Z 1
 #define FDB_TUNE_SHAPE 2
 int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value);
