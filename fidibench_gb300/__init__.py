@@ -10,3 +10,6 @@ from ._capi import FdbError, lib  # noqa: F401  (loads libfdb_upwind.so or raise
 from .upwind import Upwind  # noqa: F401
 
 __all__ = ["Upwind", "FdbError"]
+from .batch import Batch  # noqa: F401,E402
+
+__all__.append("Batch")

@@ -52,6 +52,19 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),
     "fdb_checksum_noalloc": (_int, [_vp, ctypes.c_uint64, _vp, _vp]),
+    "fdb_batch_create": (_int, [_int, _vp, ctypes.POINTER(_vp)]),
+    "fdb_batch_destroy": (_int, [_vp]),
+    "fdb_batch_count": (_int, [_vp, ctypes.POINTER(_int), _u64p]),
+    "fdb_batch_set_field": (_int, [_vp, _int, _vp, _int]),
+    "fdb_batch_get_field": (_int, [_vp, _int, _vp, _int]),
+    "fdb_batch_init_sphere": (_int, [_vp, _int, _vp, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_uint64]),
+    "fdb_batch_set_stream": (_int, [_vp, _vp]),
+    "fdb_batch_set_tuning": (_int, [_vp, _int, _int]),
+    "fdb_batch_advect": (_int, [_vp, _int, _vp]),
+    "fdb_batch_advect_looped": (_int, [_vp, _int, _vp]),
+    "fdb_batch_checksums": (_int, [_vp, _vp]),
+    "fdb_batch_autotune": (_int, [_vp, _int, _vp, ctypes.c_char_p, _vp]),
     "fdb_upwind_init_sphere": (_int, [_vp, _vp, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_uint64]),
     "fdb_upwind_adjoint": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _vp, _int, _int]),

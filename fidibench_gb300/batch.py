@@ -1,0 +1,139 @@
+"""Batches of independent upwind problems (fdb_batch_* in include/fdb_upwind.h).
+
+Each instance is one reference Upwind<ndims> problem (upwind/cxx/upwind.cxx:
+23-49, ndims <= 3) with its own grid, velocity and time step; ``advect``
+advances all of them in one persistent launch, ``advect_looped`` runs the
+single-field kernel instance by instance (the comparator).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, lib
+
+
+class InstanceDesc(ctypes.Structure):
+    _fields_ = [("ndims", ctypes.c_int), ("num_cells", ctypes.c_uint64 * 3),
+                ("velocity", ctypes.c_double * 3), ("lengths", ctypes.c_double * 3)]
+
+
+class Batch:
+    def __init__(self, instances):
+        """instances: iterable of (velocity, lengths, numCells) triples."""
+        inst = list(instances)
+        arr = (InstanceDesc * len(inst))()
+        self.shapes = []
+        for k, (v, L, n) in enumerate(inst):
+            nd = len(n)
+            if not (len(v) == len(L) == nd) or nd < 1 or nd > 3:
+                raise ValueError("each instance needs 1..3 axes of velocity, lengths, numCells")
+            arr[k].ndims = nd
+            for j in range(nd):
+                arr[k].num_cells[j] = int(n[j])
+                arr[k].velocity[j] = float(v[j])
+                arr[k].lengths[j] = float(L[j])
+            self.shapes.append(tuple(int(x) for x in n))
+        h = ctypes.c_void_p()
+        check(lib.fdb_batch_create(len(inst), arr, ctypes.byref(h)))
+        self._h = h
+        self.count = len(inst)
+        self.sizes = [int(np.prod(s)) for s in self.shapes]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.fdb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def total_cells(self) -> int:
+        c = ctypes.c_int()
+        t = ctypes.c_uint64()
+        check(lib.fdb_batch_count(self._h, ctypes.byref(c), ctypes.byref(t)))
+        return t.value
+
+    def _dts(self, dt) -> np.ndarray:
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (self.count,)))
+        return d
+
+    def advect(self, numTimeSteps: int, dt) -> None:
+        d = self._dts(dt)
+        check(lib.fdb_batch_advect(self._h, int(numTimeSteps), d.ctypes.data))
+
+    def advect_looped(self, numTimeSteps: int, dt) -> None:
+        d = self._dts(dt)
+        check(lib.fdb_batch_advect_looped(self._h, int(numTimeSteps), d.ctypes.data))
+
+    def checksums(self) -> np.ndarray:
+        out = np.empty(self.count, dtype=np.float64)
+        check(lib.fdb_batch_checksums(self._h, out.ctypes.data))
+        return out
+
+    def set_field(self, index: int, values) -> None:
+        if hasattr(values, "is_cuda") and values.is_cuda:
+            check(lib.fdb_batch_set_field(self._h, int(index), values.data_ptr(), 1))
+            return
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.float64)).reshape(-1)
+        if a.size != self.sizes[index]:
+            raise ValueError(f"instance {index} has {self.sizes[index]} cells, got {a.size}")
+        check(lib.fdb_batch_set_field(self._h, int(index), a.ctypes.data, 0))
+
+    def get_field(self, index: int) -> np.ndarray:
+        out = np.empty(self.sizes[index], dtype=np.float64)
+        check(lib.fdb_batch_get_field(self._h, int(index), out.ctypes.data, 0))
+        return out
+
+    def init_sphere(self, index: int, center, radius: float, noise_amp: float = 0.0,
+                    seed: int = 0) -> None:
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float64))
+        check(lib.fdb_batch_init_sphere(self._h, int(index), c.ctypes.data, float(radius),
+                                        float(noise_amp), int(seed)))
+
+    def set_stream(self, stream) -> None:
+        raw = getattr(stream, "cuda_stream", stream)
+        check(lib.fdb_batch_set_stream(self._h, raw))
+
+    def set_tuning(self, depth: int | None = None, shape: int | None = None,
+                   tile_z: int | None = None) -> None:
+        if depth is not None:
+            check(lib.fdb_batch_set_tuning(self._h, 3, int(depth)))
+        if shape is not None:
+            check(lib.fdb_batch_set_tuning(self._h, 2, int(shape)))
+        if tile_z is not None:
+            check(lib.fdb_batch_set_tuning(self._h, 1, int(tile_z)))
+
+    def autotune(self, numTimeSteps: int, dt, cache_path: str | None = None) -> dict:
+        d = self._dts(dt)
+        chosen = (ctypes.c_int * 3)()
+        check(lib.fdb_batch_autotune(self._h, int(numTimeSteps), d.ctypes.data,
+                                     cache_path.encode() if cache_path else None, chosen))
+        return {"depth": chosen[0], "shape": chosen[1], "tile_z": chosen[2]}
+
+
+def random_instances(count: int, seed: int, nmin: int = 32, nmax: int = 160, cfl: float = 0.5):
+    """The uneven workload of the batched benchmark: axis lengths uniform in
+    [nmin, nmax], velocities uniform in [-1, 1]^3, dt = cfl * min dx/|v|,
+    sphere centres in [0.3, 0.7]^3 and radii in [0.1, 0.25] (all seeded)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = tuple(int(x) for x in rng.integers(nmin, nmax + 1, size=3))
+        v = tuple(float(x) for x in rng.uniform(-1.0, 1.0, size=3))
+        L = (1.0, 1.0, 1.0)
+        dt = cfl * min(Lj / nj / abs(vj) for Lj, nj, vj in zip(L, n, v) if vj != 0.0)
+        centre = tuple(float(x) for x in rng.uniform(0.3, 0.7, size=3))
+        radius = float(rng.uniform(0.1, 0.25))
+        out.append({"n": n, "v": v, "L": L, "dt": dt, "center": centre, "radius": radius})
+    return out
+
+
+__all__ = ["Batch", "InstanceDesc", "random_instances"]
+_ = _capi

@@ -30,8 +30,9 @@
 // output tile of (32-K) x (R*W-K) cells in (x, y) and marches along z over tz
 // output planes after K warm-up planes.  Lanes are consecutive x (coalesced
 // 256 B row accesses), each thread holds R consecutive y rows of one column
-// in registers (shapes R x W = 8x8 and 4x16 are compiled, each with the
-// plane history in registers or in shared memory).  Per level: x-1 from lane-1 by SHFL, y-1 from the thread's
+// in registers (shapes R x W = 8x8 and 4x16 with the plane history in
+// registers or shared memory, and 4x8 with it in shared memory, are
+// compiled).  Per level: x-1 from lane-1 by SHFL, y-1 from the thread's
 // previous row (row 0 from the warp above through shared memory, one
 // __syncthreads per level), z-1 from the thread's K-deep history of the
 // previous plane.  The next plane is prefetched with cp.async into shared
@@ -52,6 +53,14 @@ namespace fdb {
 
 using fx::FixedArgs;
 using fx::ScaleSlot;
+
+double growth_bound(const Coeffs3& c) { return fabs(c.w) + c.az + c.ay + c.ax; }
+
+int guard_bits(const Coeffs3& c, int K) {
+  const double G = growth_bound(c);
+  if (G <= 1.0) return 0;
+  return (int)ceil(K * log2(G)) + 1;
+}
 
 namespace {
 
@@ -89,19 +98,15 @@ __global__ void k_slots_init(ScaleSlot* slots) {
   }
 }
 
-double growth_bound(const Coeffs3& c) { return fabs(c.w) + c.az + c.ay + c.ax; }
 
-int guard_bits(const Coeffs3& c, int K) {
-  const double G = growth_bound(c);
-  if (G <= 1.0) return 0;
-  return (int)ceil(K * log2(G)) + 1;
-}
+}  // namespace
 
-int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
-               bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err, int tz_override,
-               cudaStream_t st) {
+// Tiling and coefficients of one field for the fixed kernel (slot pointers
+// are left null).  tz_override > 0 fixes the output planes per CTA.
+fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K, int tz_override,
+                              int64_t resident_ctas) {
   const int R = fx::shape_rows(shape), W = fx::shape_warps(shape);
-  FixedArgs a;
+  FixedArgs a{};
   a.nz = (int)g.nz;
   a.ny = (int)g.ny;
   a.nx = (int)g.nx;
@@ -115,8 +120,8 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
   const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
   int tz = tz_override;
   if (tz <= 0) {
-    // about four waves of resident CTAs (8 x 152 for 256-thread CTAs)
-    const int64_t want = (int64_t)8 * 152 * 256 / (32 * W);
+    // about four waves of the resident CTAs
+    const int64_t want = 4 * resident_ctas;
     int64_t cz = (want + txy - 1) / txy;
     if (cz < 1) cz = 1;
     tz = (int)((a.nz + cz - 1) / cz);
@@ -129,10 +134,26 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
   a.qy = make_qcoeff(c.ay);
   a.qx = make_qcoeff(c.ax);
   a.guard = guard_bits(c, K);
+  return a;
+}
+
+namespace {
+
+int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
+               bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err, int tz_override,
+               int guard_K, cudaStream_t st) {
+  // 8 x 152 resident 256-thread CTAs, scaled to this shape's CTA size
+  FixedArgs a = make_fixed_args(g, c, shape, K, tz_override,
+                                (int64_t)2 * 152 * 256 / (32 * fx::shape_warps(shape)));
+  // guard bits sized for the call's full depth, also on a shorter final
+  // launch, so that every launch of a call uses the same headroom rule as the
+  // batched kernel (which sizes them once per instance)
+  a.guard = guard_bits(c, guard_K);
   a.slot_in = slots + (i % 3);
   a.slot_out = slots + ((i + 1) % 3);
   a.slot_reset = slots + ((i + 2) % 3);
   a.err = err;
+  const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
   const int64_t blocks = txy * a.tiles_z;
   if (blocks > 0x7FFFFFFF) return fail(FDB_ERR_UNSUPPORTED, "grid too large for the fixed kernel");
   const int64_t* pin = (const int64_t*)in;
@@ -141,6 +162,7 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
     case fx::kR4W16: fx::launch_r4w16(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
     case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
     case fx::kR4W16S: fx::launch_r4w16s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
+    case fx::kR4W8S: fx::launch_r4w8s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
     default: fx::launch_r8w8(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
   }
   note_launch();
@@ -212,7 +234,7 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   for (int l = 0, done = 0; l < nlaunch; ++l, ++i) {
     const int k = (steps - done) < K ? (steps - done) : K;
     FDB_TRY(launch_one(g, c, shape, k, buf[*cur], buf[*cur ^ 1], l == 0, l == nlaunch - 1, slots,
-                       i, err, tune.tz, s));
+                       i, err, tune.tz, K, s));
     *cur ^= 1;
     done += k;
   }

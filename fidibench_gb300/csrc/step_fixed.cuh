@@ -80,48 +80,30 @@ __device__ __forceinline__ int64_t update(int64_t c, int64_t zb, int64_t up, int
   return c + acc * 4;
 }
 
-// Dynamic shared memory of one CTA: plane prefetch [2][R][threads], plus the
-// K-deep plane history [K][R][threads] when HSM (history in shared memory).
+// Dynamic shared memory of one CTA: plane prefetch [2][R][threads] (cp.async
+// loader only), plus the K-deep plane history [K][R][threads] when HSM.
 template <int K, int R, int W, bool HSM>
 constexpr int fixed_smem_bytes() {
   return (2 + (HSM ? K : 0)) * R * 32 * W * (int)sizeof(int64_t);
 }
 
-// R rows per thread, W warps per CTA (stacked in y): region 32 x (R*W).
-// HSM keeps the plane history in shared memory (each thread touches only its
-// own slots, so it needs no barrier) and frees 2*K*R registers per thread for
-// row updates in flight.
-template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64>
-__global__ void __launch_bounds__(32 * W, MINB)
-k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
-  constexpr int kThreads = 32 * W;
-  extern __shared__ __align__(16) int64_t s_dyn[];
-  int64_t(*s_pre)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn);
-  int64_t(*s_hist)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn + 2 * R * kThreads);
-  __shared__ int64_t s_row[2][W][32];
-  __shared__ unsigned long long s_or[W];
-
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int warp = tid >> 5;
-  int bid = blockIdx.x;
-  const int tile_x = bid % a.tiles_x;
-  bid /= a.tiles_x;
-  const int tile_y = bid % a.tiles_y;
-  const int tile_z = bid / a.tiles_y;
-
-  // ---- scale of this launch ----------------------------------------------
-  const unsigned long long M = a.slot_in->m;
-  const int kind = a.slot_in->kind;
-  const int s_in = a.slot_in->s;
-  const int T = 58 - a.guard;  // highest bit allowed for |F| at the input
+// Scale of a launch (or, in the batched kernel, of one instance's time block)
+// from its input slot: s = scale of the fixed-point values used inside, d =
+// shift that brings int64 input (held at scale s_in) to scale s.  Returns
+// false when the slot reports a non-finite input.
+__device__ __forceinline__ bool scale_from_slot(const ScaleSlot* slot, int guard, int* s_out,
+                                                int* d_out) {
+  // L1-bypassing loads: in the persistent batched kernel the slots are
+  // rewritten by other CTAs during the launch
+  const unsigned long long M = __ldcg(&slot->m);
+  const int kind = __ldcg(&slot->kind);
+  const int s_in = __ldcg(&slot->s);
+  const int T = 58 - guard;  // highest bit allowed for |F| at the input
   int s = 0, d = 0;
+  bool ok = true;
   if (kind == 0) {
-    if (M >= 0x7FF0000000000000ull) {
-      if (tid == 0) atomicOr(a.err, 1);  // NaN/Inf in the input field
-    } else if (M != 0ull) {
-      s = T + 1023 - (int)(M >> 52);  // max|f| < 2^(E-1022)  ->  |F| < 2^(T+1)
-    }
+    if (M >= 0x7FF0000000000000ull) ok = false;  // NaN/Inf in the input field
+    else if (M != 0ull) s = T + 1023 - (int)(M >> 52);  // max|f| < 2^(E-1022) -> |F| < 2^(T+1)
   } else if (M != 0ull) {
     d = T - (63 - __clzll((long long)M));
     d = d > 62 ? 62 : (d < -62 ? -62 : d);
@@ -129,13 +111,37 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
   } else {
     s = s_in;
   }
-  if (blockIdx.x == 0 && tid == 0) {
-    a.slot_reset->m = 0ull;
-    a.slot_reset->kind = 1;
-    a.slot_out->s = s;
-    a.slot_out->kind = 1;
-  }
+  *s_out = s;
+  *d_out = d;
+  return ok;
+}
 
+// Loaders of the next plane: cp.async into shared memory (one tile per launch:
+// no other CTA writes the input during the launch), or L1-bypassing register
+// loads (the persistent batched kernel reads data that other CTAs wrote
+// earlier in the same launch, which L1 may hold stale).
+enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1 };
+
+// Advance one tile of one field by `levels` (<= K) steps.  The tile's output
+// region is x in [X0, X0+tx), y in [Y0, Y0+ty), z in [Z0, Z0+tz) of the
+// logical axes; the CTA computes a (32) x (R*W) x (tz+K) region that starts
+// K cells upstream on every axis.  my_or accumulates |F| bits of the stored
+// outputs.  Callers synchronise the CTA before reusing shared memory.
+template <int K, int R, int W, bool HSM, int LOADER>
+__device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int tile_z,
+                                             int levels, bool in_f64, bool out_f64, int s, int d,
+                                             const int64_t* __restrict__ in,
+                                             int64_t* __restrict__ out, int64_t* s_dyn,
+                                             int64_t (*s_row)[W][32],
+                                             unsigned long long& my_or) {
+  constexpr int kThreads = 32 * W;
+  int64_t(*s_pre)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn);
+  int64_t(*s_hist)[R][kThreads] =
+      reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn + (LOADER == kLoadCpAsync ? 2 : 0) * R * kThreads);
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
   const int X0 = tile_x * a.tx;
   const int Y0 = tile_y * a.ty;
   const int Z0 = tile_z * a.tz;
@@ -170,6 +176,7 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
 
   int64_t hist[HSM ? 1 : K][R];
   int64_t cur[R];
+  int64_t pre[LOADER == kLoadL2Regs ? R : 1];
 #pragma unroll
   for (int t = 0; t < (HSM ? 1 : K); ++t)
 #pragma unroll
@@ -185,38 +192,51 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
   int lz = wrap_mod(Z0 - K, a.nz);
   {
     const int64_t* src = plane_ptr(in, lz);
+    if (LOADER == kLoadCpAsync) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], src + row_off(r));
-    cp_async_commit();
+      for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], src + row_off(r));
+      cp_async_commit();
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + row_off(r));
+    }
   }
 
-  unsigned long long my_or = 0ull;
   int parity = 0;
   for (int p = 0; p < nplanes; ++p) {
     const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
-    if (p + 1 < nplanes) {
-      const int64_t* src = plane_ptr(in, lz_next);
+    if (LOADER == kLoadCpAsync) {
+      if (p + 1 < nplanes) {
+        const int64_t* src = plane_ptr(in, lz_next);
 #pragma unroll
-      for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], src + row_off(r));
-    }
-    cp_async_commit();
-    cp_async_wait<1>();
+        for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], src + row_off(r));
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int64_t raw = s_pre[p & 1][r][tid];
-      if (IN_F64) cur[r] = to_fixed(__longlong_as_double(raw), s);
-      else cur[r] = raw;
+      for (int r = 0; r < R; ++r) cur[r] = s_pre[p & 1][r][tid];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) cur[r] = pre[r];
+      if (p + 1 < nplanes) {
+        const int64_t* src = plane_ptr(in, lz_next);
+#pragma unroll
+        for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + row_off(r));
+      }
     }
-    if (!IN_F64 && d != 0) {
+    if (in_f64) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) cur[r] = to_fixed(__longlong_as_double(cur[r]), s);
+    } else if (d != 0) {
 #pragma unroll
       for (int r = 0; r < R; ++r) cur[r] = d > 0 ? (cur[r] << d) : (cur[r] >> (-d));
     }
 #pragma unroll
     for (int t = 0; t < K; ++t) {
-      // warm-up plane p holds valid levels 0..p only: level t+1 is skipped for
-      // t >= p (uniform across the CTA), but level t is still recorded as the
-      // history that level t+1 of the next plane reads
-      if (p < K && t >= p) {
+      // Level t+1 is skipped (uniformly across the CTA) on warm-up plane p
+      // for t >= p, where it is not valid, and for t >= levels; level t is
+      // still recorded as the history that level t+1 of the next plane reads.
+      if ((p < K && t >= p) || t >= levels) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if (HSM) s_hist[t][r][tid] = cur[r];
@@ -256,7 +276,7 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
         if (row_mask & (1u << r)) {
           const int64_t v = cur[r];
           my_or |= (unsigned long long)(v ^ (v >> 63));
-          if (OUT_F64)
+          if (out_f64)
             dst[row_off(r)] = __double_as_longlong(to_double(v, s));
           else
             dst[row_off(r)] = v;
@@ -265,25 +285,63 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
     }
     lz = lz_next;
   }
-  cp_async_wait<0>();
+  if (LOADER == kLoadCpAsync) cp_async_wait<0>();
+}
 
+// OR of my_or over the CTA -> atomicOr into *dst (thread 0).  Contains a
+// __syncthreads.
+template <int W>
+__device__ __forceinline__ void cta_or(unsigned long long my_or, unsigned long long* s_or,
+                                       unsigned long long* dst) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) my_or |= __shfl_xor_sync(0xffffffffu, my_or, o);
   if (lane == 0) s_or[warp] = my_or;
   __syncthreads();
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     unsigned long long m = 0ull;
 #pragma unroll
     for (int w = 0; w < W; ++w) m |= s_or[w];
-    if (m) atomicOr(&a.slot_out->m, m);
+    if (m) atomicOr(dst, m);
   }
+}
+
+// One launch = K steps of one field; one tile per CTA.
+template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64>
+__global__ void __launch_bounds__(32 * W, MINB)
+k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
+  extern __shared__ __align__(16) int64_t s_dyn[];
+  __shared__ int64_t s_row[2][W][32];
+  __shared__ unsigned long long s_or[W];
+
+  int bid = blockIdx.x;
+  const int tile_x = bid % a.tiles_x;
+  bid /= a.tiles_x;
+  const int tile_y = bid % a.tiles_y;
+  const int tile_z = bid / a.tiles_y;
+
+  int s, d;
+  if (!scale_from_slot(a.slot_in, a.guard, &s, &d) && threadIdx.x == 0) atomicOr(a.err, 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.slot_reset->m = 0ull;
+    a.slot_reset->kind = 1;
+    a.slot_out->s = s;
+    a.slot_out->kind = 1;
+  }
+  unsigned long long my_or = 0ull;
+  advance_tile<K, R, W, HSM, kLoadCpAsync>(a, tile_x, tile_y, tile_z, K, IN_F64, OUT_F64, s, d,
+                                           in, out, s_dyn, s_row, my_or);
+  cta_or<W>(my_or, s_or, &a.slot_out->m);
 }
 
 // Kernel shapes compiled into the library: rows per thread x warps per CTA,
 // history in registers (reg) or shared memory (smem).
-enum Shape { kR8W8 = 0, kR4W16 = 1, kR8W8S = 2, kR4W16S = 3, kNumShapes = 4 };
+enum Shape { kR8W8 = 0, kR4W16 = 1, kR8W8S = 2, kR4W16S = 3, kR4W8S = 4, kNumShapes = 5 };
 constexpr int shape_rows(int sh) { return (sh == kR8W8 || sh == kR8W8S) ? 8 : 4; }
-constexpr int shape_warps(int sh) { return (sh == kR8W8 || sh == kR8W8S) ? 8 : 16; }
+constexpr int shape_warps(int sh) {
+  return (sh == kR8W8 || sh == kR8W8S || sh == kR4W8S) ? 8 : 16;
+}
 
 template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT>
 void launch_k(unsigned blocks, const int64_t* in, int64_t* out, const FixedArgs& a,
@@ -318,6 +376,13 @@ void launch_shape(int K, bool in_f64, bool out_f64, unsigned blocks, const int64
   }
 }
 
+// defined in step_fixed.cu
+}  // namespace fx
+fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K, int tz_override,
+                              int64_t resident_ctas);
+int guard_bits(const Coeffs3& c, int K);
+namespace fx {
+
 // defined in step_fixed_<shape>.cu
 #define FDB_FX_DECLARE(NAME)                                                               \
   void NAME(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,          \
@@ -326,6 +391,7 @@ FDB_FX_DECLARE(launch_r8w8)
 FDB_FX_DECLARE(launch_r4w16)
 FDB_FX_DECLARE(launch_r8w8s)
 FDB_FX_DECLARE(launch_r4w16s)
+FDB_FX_DECLARE(launch_r4w8s)
 #undef FDB_FX_DECLARE
 
 }  // namespace fx

@@ -1,0 +1,15 @@
+// step_fixed_r4w8s.cu -- instantiations of the fixed-point kernel: 4 rows per
+// thread, 8 warps per CTA, plane history in shared memory (a separate
+// translation unit so that the shapes compile in parallel).
+#include "step_fixed.cuh"
+
+namespace fdb {
+namespace fx {
+
+void launch_r4w8s(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+                 int64_t* out, const FixedArgs& a, cudaStream_t st) {
+  launch_shape<4, 8, true, 2>(K, in_f64, out_f64, blocks, in, out, a, st);
+}
+
+}  // namespace fx
+}  // namespace fdb

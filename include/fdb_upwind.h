@@ -104,9 +104,11 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
  *  FDB_TUNE_TILE_Z : output planes per CTA along the slowest axis (0 = auto).
  *  FDB_TUNE_SHAPE  : rows per thread x warps per CTA and where the plane
  *                    history lives: 0 = 8x8 registers, 1 = 4x16 registers,
- *                    2 = 8x8 shared memory, 3 = 4x16 shared memory (-1 = auto). */
+ *                    2 = 8x8 shared memory, 3 = 4x16 shared memory,
+ *                    4 = 4x8 shared memory (-1 = auto). */
 #define FDB_TUNE_TILE_Z 1
 #define FDB_TUNE_SHAPE 2
+#define FDB_TUNE_DEPTH 3 /* batches only: steps per time block (0 = auto, 2..4) */
 int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value);
 
 /* Number of cells, and the arithmetic the last advect actually used. */
@@ -138,6 +140,46 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
 int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
                             const double* lam_in_dev, double* lam_out_dev,
                             double* dcoef_host);
+
+/* ---------------------------------------------------------------------------
+ * Batches (no reference counterpart): many independent Upwind problems of
+ * uneven sizes and velocities, each one the reference's Upwind<ndims>
+ * (upwind.cxx:23-49) with ndims <= 3, advanced together.
+ * fdb_batch_advect runs one persistent launch per call (all instances, all
+ * time blocks, per-instance dependency tracking with bounded waits; replayed
+ * from a CUDA graph when called again with the same steps, dt and tuning).
+ * fdb_batch_advect_looped is the comparator: the single-field kernel looped
+ * over the instances.  dt holds one time step per instance.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int ndims;              /* 1..3 */
+  uint64_t num_cells[3];  /* first ndims entries used */
+  double velocity[3];
+  double lengths[3];
+} fdb_instance_desc;
+
+typedef struct fdb_batch fdb_batch;
+
+/* Each instance starts with f = 0, f[0] = 1 (upwind.cxx:45-48). */
+int fdb_batch_create(int count, const fdb_instance_desc* descs, fdb_batch** out);
+int fdb_batch_destroy(fdb_batch* b);
+int fdb_batch_count(fdb_batch* b, int* count, uint64_t* total_cells);
+int fdb_batch_set_field(fdb_batch* b, int index, const double* src, int is_device);
+int fdb_batch_get_field(fdb_batch* b, int index, double* dst, int is_device);
+int fdb_batch_init_sphere(fdb_batch* b, int index, const double* center, double radius,
+                          double noise_amp, uint64_t seed);
+int fdb_batch_set_stream(fdb_batch* b, void* cuda_stream);
+/* keys FDB_TUNE_DEPTH, FDB_TUNE_SHAPE (2, 3 or 4), FDB_TUNE_TILE_Z */
+int fdb_batch_set_tuning(fdb_batch* b, int key, int value);
+int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt);
+int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt);
+/* checksum() of every instance (upwind.cxx:91-93) into out[count]; synchronises. */
+int fdb_batch_checksums(fdb_batch* b, double* out);
+/* Times the compiled (depth, shape, tile_z) choices on a copy of the fields
+ * and keeps the fastest; with cache_path, reuses/stores the choice per problem
+ * class.  chosen (nullable) receives {depth, shape, tile_z}. */
+int fdb_batch_autotune(fdb_batch* b, int num_steps, const double* dt, const char* cache_path,
+                       int* chosen);
 
 /* ---------------------------------------------------------------------------
  * Checksum without any allocation.  No counterpart in the reference: it exists

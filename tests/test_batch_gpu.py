@@ -1,0 +1,131 @@
+"""Batched form through the C-ABI: every instance against the oracle, the
+persistent launch bit-identical to the single-field kernel looped over the
+instances, graph replay, tuning choices, and the bounded-wait error path."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_maxnorm
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-13
+SUM_TOL = 1e-12
+
+
+def make_batch(fdb, specs, seed=3):
+    b = fdb.Batch([(s["v"], s["L"], s["n"]) for s in specs])
+    for k, s in enumerate(specs):
+        b.init_sphere(k, s["center"], s["radius"], 0.01, seed + k)
+    return b
+
+
+def small_specs(count=9, seed=5, nmin=5, nmax=40):
+    from fidibench_gb300.batch import random_instances
+    return random_instances(count, seed, nmin, nmax)
+
+
+def test_batched_matches_oracle(fdb, port):
+    specs = small_specs()
+    b = make_batch(fdb, specs)
+    f0 = [b.get_field(k) for k in range(b.count)]
+    dts = [s["dt"] for s in specs]
+    steps = 11
+    b.advect(steps, dts)
+    sums = b.checksums()
+    for k, s in enumerate(specs):
+        ref = port.advect(s["n"], s["v"], s["L"], f0[k], steps, s["dt"])
+        assert rel_maxnorm(b.get_field(k), ref) <= FIELD_TOL, k
+        assert sums[k] == pytest.approx(port.checksum(ref), rel=SUM_TOL)
+    b.close()
+
+
+@pytest.mark.parametrize("depth,shape,tile_z", [(4, -1, 0), (2, 3, 0), (3, 2, 8), (4, 4, 5)])
+def test_batched_bit_identical_to_looped(fdb, depth, shape, tile_z):
+    specs = small_specs(count=7, seed=11, nmin=20, nmax=70)
+    dts = [s["dt"] for s in specs]
+    a = make_batch(fdb, specs)
+    c = make_batch(fdb, specs)
+    a.set_tuning(depth=depth, shape=shape, tile_z=tile_z)
+    for _ in range(2):  # the second call replays the captured graph
+        a.advect(21, dts)
+        c.advect_looped(21, dts)
+    # integer arithmetic: any tiling gives the same field; the looped
+    # comparator runs 4 steps per launch, so equal time blocks are bit-equal
+    for k in range(a.count):
+        if depth == 4:
+            assert np.array_equal(a.get_field(k), c.get_field(k)), k
+        else:
+            assert rel_maxnorm(a.get_field(k), c.get_field(k)) <= FIELD_TOL, k
+    a.close()
+    c.close()
+
+
+def test_batched_any_depth_matches_oracle(fdb, port):
+    specs = small_specs(count=5, seed=13, nmin=8, nmax=33)
+    dts = [s["dt"] for s in specs]
+    for depth in (2, 3, 4):
+        b = make_batch(fdb, specs)
+        f0 = [b.get_field(k) for k in range(b.count)]
+        b.set_tuning(depth=depth)
+        b.advect(10, dts)
+        for k, s in enumerate(specs):
+            ref = port.advect(s["n"], s["v"], s["L"], f0[k], 10, s["dt"])
+            assert rel_maxnorm(b.get_field(k), ref) <= FIELD_TOL, (depth, k)
+        b.close()
+
+
+def test_autotune_keeps_results_and_caches(fdb, tmp_path, port):
+    specs = small_specs(count=6, seed=17, nmin=16, nmax=48)
+    dts = [s["dt"] for s in specs]
+    b = make_batch(fdb, specs)
+    f0 = [b.get_field(k) for k in range(b.count)]
+    cache = str(tmp_path / "tune.txt")
+    chosen = b.autotune(8, dts, cache)
+    assert chosen["depth"] in (2, 3, 4)
+    for k in range(b.count):  # the autotuner restores the fields
+        assert np.array_equal(b.get_field(k), f0[k])
+    again = b.autotune(8, dts, cache)  # from the cache
+    assert again == chosen
+    b.advect(8, dts)
+    for k, s in enumerate(specs):
+        ref = port.advect(s["n"], s["v"], s["L"], f0[k], 8, s["dt"])
+        assert rel_maxnorm(b.get_field(k), ref) <= FIELD_TOL
+    b.close()
+
+
+def test_bounded_wait_expires_with_error_and_context_survives(fdb, monkeypatch):
+    """FDB_FAULT=timeout makes every dependency unsatisfiable with a ~1 ms
+    wait budget: the kernel must give up, report FDB_ERR_TIMEOUT, and leave
+    the context usable."""
+    specs = small_specs(count=3, seed=19, nmin=30, nmax=40)
+    dts = [s["dt"] for s in specs]
+    b = make_batch(fdb, specs)
+    monkeypatch.setenv("FDB_FAULT", "timeout")
+    b.advect(12, dts)
+    with pytest.raises(fdb.FdbError) as ei:
+        b.checksums()
+    assert ei.value.code == 5
+    monkeypatch.delenv("FDB_FAULT")
+    for k, s in enumerate(specs):
+        b.init_sphere(k, s["center"], s["radius"], 0.0, 1)
+    b.advect(12, dts)
+    assert np.all(np.isfinite(b.checksums()))
+    b.close()
+
+
+def test_unsupported_instance_falls_back(fdb, port):
+    # a Courant number above 1 on one instance: the batch loops the FP64 path
+    specs = small_specs(count=3, seed=23, nmin=10, nmax=20)
+    specs[1] = dict(specs[1], dt=specs[1]["dt"] * 3.0)
+    dts = [s["dt"] for s in specs]
+    b = make_batch(fdb, specs)
+    f0 = [b.get_field(k) for k in range(b.count)]
+    b.advect(5, dts)
+    for k, s in enumerate(specs):
+        ref = port.advect(s["n"], s["v"], s["L"], f0[k], 5, s["dt"])
+        assert rel_maxnorm(b.get_field(k), ref) <= FIELD_TOL
+    b.close()
