@@ -48,6 +48,7 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_checksum": (_int, [_vp, _dp]),
     "fdb_upwind_std": (_int, [_vp, _dp]),
     "fdb_upwind_set_stream": (_int, [_vp, _vp]),
+    "fdb_upwind_set_velocity": (_int, [_vp, _vp]),
     "fdb_upwind_set_arith": (_int, [_vp, _int, _int]),
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),

@@ -340,6 +340,15 @@ int fdb_upwind_std(fdb_upwind* h, double* out) {
   return FDB_OK;
 }
 
+int fdb_upwind_set_velocity(fdb_upwind* h, const double* velocity) {
+  FDB_TRY(check_handle(h));
+  if (!velocity) return fail(FDB_ERR_INVALID, "null velocity");
+  Geom g;
+  FDB_TRY(make_geom(h->g.ndims, velocity, h->g.L, h->g.n, &g));
+  h->g = g;
+  return FDB_OK;
+}
+
 int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream) {
   FDB_TRY(check_handle(h));
   FDB_TRY(sync(h));

@@ -86,6 +86,15 @@ class Upwind:
         memory), -1 = automatic."""
         check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
 
+    def set_velocity(self, velocity) -> None:
+        """New velocity for the same grid (the upwind directions follow its sign)."""
+        v = _as_f64(velocity)
+        if v.size != self.ndims:
+            raise ValueError("velocity needs one value per axis")
+        check(lib.fdb_upwind_set_velocity(self._h, v.ctypes.data))
+        self.v = v
+        self.upDirection = np.where(self.v < 0.0, 1, -1).astype(np.int32)
+
     def set_stream(self, stream) -> None:
         """Enqueue on a CUDA stream (a torch.cuda.Stream, a raw handle or None)."""
         raw = getattr(stream, "cuda_stream", stream)

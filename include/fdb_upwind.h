@@ -93,6 +93,11 @@ int fdb_upwind_checksum(fdb_upwind* h, double* out);
 /* Replaces std() -- upwind.cxx:95-103 (population standard deviation). */
 int fdb_upwind_std(fdb_upwind* h, double* out);
 
+/* Replace the velocity (ndims values) of an existing problem, re-deriving the
+ * upwind directions as the constructor does (upwind.cxx:34-35); the field is
+ * kept.  Lets optimisation loops reuse one handle. */
+int fdb_upwind_set_velocity(fdb_upwind* h, const double* velocity);
+
 /* Stream to enqueue on (a cudaStream_t; NULL restores the handle's own). */
 int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream);
 
