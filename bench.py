@@ -238,6 +238,122 @@ def bench_batched(steps: int, warmup: int, stream) -> dict:
             "checksum_rel_diff_batched_vs_looped": agree}
 
 
+ADJ_N = 256
+ADJ_STEPS = 200
+ADJ_CKPT = 20
+ADJ_V = (0.8, 0.5, -0.6)
+
+
+def gaussian_random_field(n: int, corr_cells: float, seed: int, device):
+    """Seeded Gaussian random field on the periodic n^3 grid: white noise
+    smoothed by a Gaussian of standard deviation `corr_cells` cells (FFT),
+    normalised to unit standard deviation."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    w = torch.randn((n, n, n), generator=g, device=device, dtype=torch.float64)
+    k = torch.fft.fftfreq(n, device=device, dtype=torch.float64)
+    kr = torch.fft.rfftfreq(n, device=device, dtype=torch.float64)
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2
+    filt = torch.exp(-2.0 * (np.pi ** 2) * (corr_cells ** 2) * k2)
+    f = torch.fft.irfftn(torch.fft.rfftn(w) * filt, s=(n, n, n))
+    return (f - f.mean()) / f.std()
+
+
+def bench_adjoint(stream) -> dict:
+    """Adjoint form: 256^3, v = (0.8, 0.5, -0.6), dt = 0.5 min dx/|v|, 200
+    steps, checkpoints every 20; L = 0.5 ||f_T - target||^2 with a seeded
+    Gaussian random field target (correlation length 8 cells).  Reports the
+    adjoint/forward per-step cost, the dot-product test and central finite
+    differences (h = 1e-6) on 16 seeded directions and the 3 velocities."""
+    import torch
+    import fidibench_gb300 as fdb
+
+    n3 = (ADJ_N,) * 3
+    L = (1.0, 1.0, 1.0)
+    dt = 0.5 * min(1.0 / ADJ_N / abs(v) for v in ADJ_V)
+    up = fdb.Upwind(ADJ_V, L, n3)
+    up.set_stream(stream)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    up.init_sphere((0.5, 0.5, 0.5), 0.2, 0.01, SEED)
+    f0 = torch.empty(ADJ_N ** 3, dtype=torch.float64, device=dev)
+    up.get_field(f0)
+    target = gaussian_random_field(ADJ_N, 8.0, SEED, dev).reshape(-1)
+
+    def forward(x, vel=ADJ_V):
+        up.set_velocity(vel)
+        up.set_field(x)
+        up.advect(ADJ_STEPS, dt)
+        out = torch.empty_like(x)
+        up.get_field(out)
+        return out
+
+    # forward step cost (the production advect)
+    for _ in range(2):
+        forward(f0)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    up.set_field(f0)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(3):
+        up.advect(ADJ_STEPS, dt)
+    e1.record(stream)
+    e1.synchronize()
+    fwd_ms_step = e0.elapsed_time(e1) / (3 * ADJ_STEPS)
+
+    lam = forward(f0) - target
+    timings = []
+    for _ in range(2):
+        up.set_field(f0)
+        g0, gv = up.adjoint(ADJ_STEPS, dt, lam, checkpoint_every=ADJ_CKPT)
+        timings.append(up.adjoint_timings())
+    t = timings[-1]
+
+    h = 1e-6
+
+    def fd(fp, fm):
+        rp, rm = fp - target, fm - target
+        return float(torch.sum((rp - rm) * (rp + rm)).item()) / (4.0 * h)
+
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + 1)
+    errs_f0 = []
+    for _ in range(16):
+        dvec = torch.randn(f0.shape, generator=gen, device=dev, dtype=torch.float64)
+        exact = float(torch.dot(g0, dvec).item())
+        errs_f0.append(abs(fd(forward(f0 + h * dvec), forward(f0 - h * dvec)) - exact) /
+                       max(abs(exact), 1e-300))
+    errs_v = []
+    for j in range(3):
+        vp, vm = list(ADJ_V), list(ADJ_V)
+        vp[j] += h
+        vm[j] -= h
+        est = fd(forward(f0, vp), forward(f0, vm))
+        errs_v.append(abs(est - gv[j]) / max(abs(gv[j]), 1e-300))
+    up.set_velocity(ADJ_V)
+    # dot-product test <A x, y> = <x, A^T y>
+    x = torch.randn(f0.shape, generator=gen, device=dev, dtype=torch.float64)
+    y = torch.randn(f0.shape, generator=gen, device=dev, dtype=torch.float64)
+    ax = forward(x)
+    up.set_field(x)
+    aty, _ = up.adjoint(ADJ_STEPS, dt, y, checkpoint_every=ADJ_CKPT)
+    lhs = float(torch.dot(ax, y).item())
+    rhs = float(torch.dot(x, aty).item())
+    up.close()
+    adj_step = t["adjoint_ms"] / ADJ_STEPS
+    rec_step = t["recompute_ms"] / ADJ_STEPS
+    a_sum = sum(abs(v) * dt * ADJ_N for v in ADJ_V)
+    return {"workload": "adjoint_256cube_200steps_ckpt20", "dt": dt,
+            "courant_sum": a_sum, "forward_ms_per_step": fwd_ms_step,
+            "adjoint_ms_per_step": adj_step, "recompute_ms_per_step": rec_step,
+            "adjoint_over_forward": adj_step / fwd_ms_step,
+            "backward_incl_recompute_over_forward": (adj_step + rec_step) / fwd_ms_step,
+            "adjoint_gcups": ADJ_N ** 3 / (adj_step * 1e-3) / 1e9,
+            "fd_max_rel_err_f0_16dirs": max(errs_f0), "fd_max_rel_err_velocity": max(errs_v),
+            "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "grad_v": [float(x) for x in gv]}
+
+
 def run_reference_arm(args, ws, rank) -> None:
     if rank != 0:
         return
@@ -274,6 +390,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-looped leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--n", type=int, default=512, help="cube size (profiling only)")
     ap.add_argument("--tz", type=int, default=0, help="fixed kernel z-tile override")
     ap.add_argument("--shape", type=int, default=-1, help="fixed kernel CTA shape (0..2)")
@@ -377,6 +494,9 @@ def main() -> None:
     batched = None
     if not args.no_batch:
         batched = bench_batched(max(3, min(args.steps, 5)), 3, stream)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = bench_adjoint(stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -405,6 +525,7 @@ def main() -> None:
             "clocks": clk,
             "gpu_launches": launches,
             "batched": batched,
+            "adjoint": adjoint,
         }
         print(json.dumps(line))
     if dist is not None:

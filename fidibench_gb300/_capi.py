@@ -70,6 +70,7 @@ SIGNATURES: dict[str, tuple] = {
                                       ctypes.c_uint64]),
     "fdb_upwind_adjoint": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _vp, _int, _int]),
     "fdb_upwind_adjoint_step": (_int, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
+    "fdb_upwind_adjoint_timings": (_int, [_vp, _vp]),
 }
 
 

@@ -79,6 +79,8 @@ class Batch:
 
     def set_field(self, index: int, values) -> None:
         if hasattr(values, "is_cuda") and values.is_cuda:
+            import torch
+            torch.cuda.current_stream(values.device).synchronize()  # torch's writes first
             check(lib.fdb_batch_set_field(self._h, int(index), values.data_ptr(), 1))
             return
         a = np.ascontiguousarray(np.asarray(values, dtype=np.float64)).reshape(-1)

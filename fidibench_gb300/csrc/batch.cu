@@ -373,6 +373,7 @@ int make_plan(fdb_batch* b, int steps, const double* dt, int K, int shape, int t
     // per instance: whole z extent per tile unless tz is given (many small
     // instances already fill the device)
     I.a = make_fixed_args(g, c, shape, K, tz > 0 ? tz : (int)g.nz, resident);
+    I.a.scale_log = nullptr;
     I.offset = b->offsets[i];
     const int64_t items = (int64_t)I.a.tiles_x * I.a.tiles_y * I.a.tiles_z;
     if (items > (1 << 24)) return fail(FDB_ERR_UNSUPPORTED, "instance has too many tiles");

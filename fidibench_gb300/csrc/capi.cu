@@ -39,6 +39,11 @@ struct fdb_upwind {
   std::vector<double*> ckpt;
   std::vector<double*> seg;
   double* lam[2] = {nullptr, nullptr};
+  double* adj_dpart = nullptr;  // fixed-point adjoint: per-CTA contraction slots
+  int adj_dpart_cap = 0;
+  double* adj_scratch = nullptr;
+  size_t adj_scratch_bytes = 0;
+  double adj_ms[3] = {0.0, 0.0, 0.0};  // last adjoint: forward, recompute, transposed steps
 };
 
 namespace fdb {
@@ -157,6 +162,12 @@ void free_adjoint(fdb_upwind* h) {
     if (h->lam[k]) cudaFree(h->lam[k]);
     h->lam[k] = nullptr;
   }
+  if (h->adj_dpart) cudaFree(h->adj_dpart);
+  if (h->adj_scratch) cudaFree(h->adj_scratch);
+  h->adj_dpart = nullptr;
+  h->adj_scratch = nullptr;
+  h->adj_dpart_cap = 0;
+  h->adj_scratch_bytes = 0;
 }
 
 int dalloc(double** p, size_t count) {
@@ -398,6 +409,13 @@ int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius, d
   return sync(h);
 }
 
+int fdb_upwind_adjoint_timings(fdb_upwind* h, double* ms3) {
+  FDB_TRY(check_handle(h));
+  if (!ms3) return fail(FDB_ERR_INVALID, "null output");
+  for (int k = 0; k < 3; ++k) ms3[k] = h->adj_ms[k];
+  return FDB_OK;
+}
+
 int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
                             const double* lam_in_dev, double* lam_out_dev, double* dcoef_host) {
   FDB_TRY(check_handle(h));
@@ -433,16 +451,21 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   if (K > std::max(S, 1)) K = std::max(S, 1);
   const int nseg = (S + K - 1) / K;
   const size_t bytes = g.ntot * sizeof(double);
-  // The recompute must reproduce the forward states exactly, so the whole
-  // adjoint uses a per-step FP64 arithmetic (the fixed-point kernel only
-  // materialises every depth-th state).
-  const int arith = (h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA;
+  const Coeffs3 c = coeffs3(g, dt);
+  // Default: the fixed-point adjoint (forward and recompute on the integer
+  // pipes).  EXACT/FMA requests, or coefficients outside the fixed kernel's
+  // domain, use the FP64 adjoint with FP64 recompute.
+  const bool fixed = (h->arith == FDB_ARITH_AUTO || h->arith == FDB_ARITH_FIXED) &&
+                     fixed_supported(g, c, 1) == FDB_OK &&
+                     fixed_supported(g, c, h->depth) == FDB_OK;
+  const int arith = fixed ? FDB_ARITH_FIXED
+                          : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
 
-  // storage: nseg checkpoints, K-1 segment states, two adjoint buffers
-  if ((int)h->ckpt.size() < nseg || (int)h->seg.size() < K - 1 || !h->lam[0]) {
+  // storage: nseg checkpoints, K segment states, two adjoint buffers
+  if ((int)h->ckpt.size() < nseg || (int)h->seg.size() < K || !h->lam[0]) {
     free_adjoint(h);
     h->ckpt.assign(nseg, nullptr);
-    h->seg.assign(std::max(K - 1, 0), nullptr);
+    h->seg.assign(K, nullptr);
     int rc = FDB_OK;
     for (auto& p : h->ckpt)
       if (!rc) rc = dalloc(&p, g.ntot);
@@ -455,47 +478,141 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
       return rc;
     }
   }
-  const Coeffs3 c = coeffs3(g, dt);
   // forward with checkpoints: ckpt[s] = f^{sK}
+  cudaEvent_t fe0, fe1;
+  cudaEventCreate(&fe0);
+  cudaEventCreate(&fe1);
+  cudaEventRecord(fe0, h->stream);
   for (int s = 0; s < nseg; ++s) {
     FDB_CUDA_TRY(cudaMemcpyAsync(h->ckpt[s], h->buf[h->cur], bytes, cudaMemcpyDeviceToDevice,
                                  h->stream));
     const int len = std::min(K, S - s * K);
     FDB_TRY(advance(h, len, dt, arith));
   }
-  // backward
-  int lc = 0;
-  FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[lc], lambda_T, bytes,
-                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                               h->stream));
-  FDB_CUDA_TRY(cudaMemsetAsync(h->dpart, 0, 3 * adjoint_blocks() * sizeof(double), h->stream));
-  for (int s = nseg - 1; s >= 0; --s) {
-    const int len = std::min(K, S - s * K);
-    // states f^{sK+1} .. f^{sK+len-1} into seg[0 .. len-2]
-    const double* prev = h->ckpt[s];
-    for (int k = 1; k < len; ++k) {
-      FDB_TRY(launch_step_f64(g, c, arith, prev, h->seg[k - 1], h->stream));
-      prev = h->seg[k - 1];
+  cudaEventRecord(fe1, h->stream);
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rec_ev, adj_ev;
+  auto collect_times = [&]() {
+    float ms = 0.f;
+    h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
+    if (cudaEventElapsedTime(&ms, fe0, fe1) == cudaSuccess) h->adj_ms[0] = ms;
+    for (auto& e : rec_ev) {
+      if (cudaEventElapsedTime(&ms, e.first, e.second) == cudaSuccess) h->adj_ms[1] += ms;
     }
-    for (int k = len - 1; k >= 0; --k) {
-      const double* fk = (k == 0) ? h->ckpt[s] : h->seg[k - 1];
-      FDB_TRY(launch_adjoint_step(g, c, fk, h->lam[lc], h->lam[lc ^ 1], h->dpart, h->stream));
-      lc ^= 1;
+    for (auto& e : adj_ev) {
+      if (cudaEventElapsedTime(&ms, e.first, e.second) == cudaSuccess) h->adj_ms[2] += ms;
+      cudaEventDestroy(e.second);
     }
+    for (auto& e : rec_ev) cudaEventDestroy(e.first);
+    for (auto& e : rec_ev) cudaEventDestroy(e.second);
+    cudaEventDestroy(fe0);
+    cudaEventDestroy(fe1);
+    cudaGetLastError();
+  };
+  const int jj[3] = {g.jz, g.jy, g.jx};
+  double dda[3] = {0.0, 0.0, 0.0};  // dL/da (internal axes z, y, x)
+
+  if (fixed) {
+    const int ctas = adjoint_fixed_ctas(g, c);
+    const size_t sb = adjoint_fixed_scratch_bytes(K);
+    if (h->adj_dpart_cap < ctas || h->adj_scratch_bytes < sb) {
+      if (h->adj_dpart) cudaFree(h->adj_dpart);
+      if (h->adj_scratch) cudaFree(h->adj_scratch);
+      h->adj_dpart = nullptr;
+      h->adj_scratch = nullptr;
+      h->adj_dpart_cap = 0;
+      h->adj_scratch_bytes = 0;
+      FDB_TRY(dalloc(&h->adj_dpart, 3 * (size_t)ctas));
+      FDB_TRY(dalloc(&h->adj_scratch, (sb + 7) / 8));
+      h->adj_dpart_cap = ctas;
+      h->adj_scratch_bytes = (sb + 7) / 8 * 8;
+      FDB_CUDA_TRY(cudaMemsetAsync(h->adj_scratch, 0, h->adj_scratch_bytes, h->stream));
+    }
+    // the field's partner buffer is free after the forward pass: it holds
+    // lam_T (host input) and then dL/df0 (host output)
+    double* tmp = h->buf[h->cur ^ 1];
+    const double* lamT = lambda_T;
+    if (!is_device) {
+      FDB_CUDA_TRY(cudaMemcpyAsync(tmp, lambda_T, bytes, cudaMemcpyHostToDevice, h->stream));
+      lamT = tmp;
+    }
+    AdjointFixedIO io;
+    io.g = &g;
+    io.c = &c;
+    io.S = S;
+    io.K = K;
+    io.nseg = nseg;
+    io.ckpt = h->ckpt.data();
+    io.states = (int64_t* const*)h->seg.data();
+    io.lam[0] = (int64_t*)h->lam[0];
+    io.lam[1] = (int64_t*)h->lam[1];
+    io.lam_T = lamT;
+    io.grad_f0 = is_device ? grad_f0 : tmp;
+    io.dpart = h->adj_dpart;
+    io.dpart_cap = h->adj_dpart_cap;
+    io.dda3 = h->dscal;
+    io.scratch = h->adj_scratch;
+    io.recompute_ev = &rec_ev;
+    io.adjoint_ev = &adj_ev;
+    FDB_TRY(adjoint_fixed_run(io, h->stream));
+    if (!is_device)
+      FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FDB_TRY(sync(h));
+    collect_times();
+    int herr = 0;
+    FDB_CUDA_TRY(cudaMemcpy(&herr, (char*)h->adj_scratch + 6 * 16, sizeof(int),
+                            cudaMemcpyDeviceToHost));
+    if (herr) {
+      cudaMemset((char*)h->adj_scratch + 6 * 16, 0, sizeof(int));
+      return fail(FDB_ERR_NONFINITE, "adjoint: lambda_T or the field holds NaN or Inf");
+    }
+    for (int k = 0; k < 3; ++k) dda[k] = h->hscal[k];
+  } else {
+    // backward in FP64; the recompute repeats the forward's per-step arithmetic
+    int lc = 0;
+    FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[lc], lambda_T, bytes,
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 h->stream));
+    FDB_CUDA_TRY(cudaMemsetAsync(h->dpart, 0, 3 * adjoint_blocks() * sizeof(double), h->stream));
+    cudaEvent_t be0, be1;
+    cudaEventCreate(&be0);
+    cudaEventCreate(&be1);
+    cudaEventRecord(be0, h->stream);
+    adj_ev.push_back({be0, be1});
+    rec_ev.clear();
+    for (int s = nseg - 1; s >= 0; --s) {
+      const int len = std::min(K, S - s * K);
+      // states f^{sK+1} .. f^{sK+len-1} into seg[0 .. len-2]
+      const double* prev = h->ckpt[s];
+      for (int k = 1; k < len; ++k) {
+        FDB_TRY(launch_step_f64(g, c, arith, prev, h->seg[k - 1], h->stream));
+        prev = h->seg[k - 1];
+      }
+      for (int k = len - 1; k >= 0; --k) {
+        const double* fk = (k == 0) ? h->ckpt[s] : h->seg[k - 1];
+        FDB_TRY(launch_adjoint_step(g, c, fk, h->lam[lc], h->lam[lc ^ 1], h->dpart, h->stream));
+        lc ^= 1;
+      }
+    }
+    cudaEventRecord(be1, h->stream);
+    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], bytes,
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FDB_TRY(launch_adjoint_finish(h->dpart, h->dscal, h->stream));
+    FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FDB_TRY(sync(h));
+    collect_times();
+    cudaEventDestroy(be0);
+    // the FP64 kernel accumulates dL/dc = -dL/da
+    for (int k = 0; k < 3; ++k) dda[k] = -h->hscal[k];
   }
-  FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], bytes,
-                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                               h->stream));
-  FDB_TRY(launch_adjoint_finish(h->dpart, h->dscal, h->stream));
-  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
-                               h->stream));
-  FDB_TRY(sync(h));
   if (grad_v) {
-    // c_j = dt v_j up_j / dx_j  =>  dL/dv_j = dL/dc_j * dt up_j / dx_j
+    // a_j = -c_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j * (-dt up_j / dx_j)
     for (int j = 0; j < g.ndims; ++j) grad_v[j] = 0.0;
-    const int jj[3] = {g.jz, g.jy, g.jx};
     for (int k = 0; k < 3; ++k)
-      if (jj[k] >= 0) grad_v[jj[k]] = h->hscal[k] * (dt * (double)g.up[jj[k]] / g.dx[jj[k]]);
+      if (jj[k] >= 0) grad_v[jj[k]] = dda[k] * (-dt * (double)g.up[jj[k]] / g.dx[jj[k]]);
   }
   return FDB_OK;
 }

@@ -5,6 +5,8 @@
 #include <stdint.h>
 
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "fdb_upwind.h"
 
@@ -115,5 +117,31 @@ int launch_adjoint_step(const Geom& g, const Coeffs3& c, const double* f,
                         const double* lam_in, double* lam_out, double* dpart,
                         cudaStream_t s);
 int launch_adjoint_finish(const double* dpart, double* d_out3, cudaStream_t s);
+
+// Fixed-point adjoint of a whole advect (adjoint_fixed.cu).  The forward
+// checkpoints ckpt[0..nseg) (FP64, every K steps) must already exist.
+struct AdjointFixedIO {
+  const Geom* g;
+  const Coeffs3* c;
+  int S;      // steps
+  int K;      // checkpoint interval
+  int nseg;   // ceil(S / K)
+  double* const* ckpt;
+  int64_t* const* states;  // K int64 buffers for one recomputed segment
+  int64_t* lam[2];         // adjoint ping-pong (int64)
+  const double* lam_T;     // device, FP64
+  double* grad_f0;         // device, FP64
+  double* dpart;           // 3 doubles per adjoint CTA
+  int dpart_cap;           // CTAs the buffer holds
+  double* dda3;            // device [3]: dL/da for the internal (z, y, x) axes
+  void* scratch;           // adjoint_fixed_scratch_bytes(K) bytes
+  // nullable: event pairs bracketing each recompute / transposed-step block,
+  // for the caller to read after it synchronises
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* recompute_ev = nullptr;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* adjoint_ev = nullptr;
+};
+size_t adjoint_fixed_scratch_bytes(int seg_len);
+int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c);
+int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st);
 
 }  // namespace fdb

@@ -137,11 +137,9 @@ fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K,
   return a;
 }
 
-namespace {
-
-int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
-               bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err, int tz_override,
-               int guard_K, cudaStream_t st) {
+int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
+                     bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err,
+                     int tz_override, int guard_K, int* scale_log, cudaStream_t st) {
   // 8 x 152 resident 256-thread CTAs, scaled to this shape's CTA size
   FixedArgs a = make_fixed_args(g, c, shape, K, tz_override,
                                 (int64_t)2 * 152 * 256 / (32 * fx::shape_warps(shape)));
@@ -153,6 +151,7 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
   a.slot_out = slots + ((i + 1) % 3);
   a.slot_reset = slots + ((i + 2) % 3);
   a.err = err;
+  a.scale_log = scale_log;
   const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
   const int64_t blocks = txy * a.tiles_z;
   if (blocks > 0x7FFFFFFF) return fail(FDB_ERR_UNSUPPORTED, "grid too large for the fixed kernel");
@@ -169,6 +168,8 @@ int launch_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in
   FDB_CUDA_TRY(cudaGetLastError());
   return FDB_OK;
 }
+
+namespace {
 
 int default_depth() { return kMaxDepth; }
 
@@ -233,8 +234,8 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   int i = i0;
   for (int l = 0, done = 0; l < nlaunch; ++l, ++i) {
     const int k = (steps - done) < K ? (steps - done) : K;
-    FDB_TRY(launch_one(g, c, shape, k, buf[*cur], buf[*cur ^ 1], l == 0, l == nlaunch - 1, slots,
-                       i, err, tune.tz, K, s));
+    FDB_TRY(launch_fixed_one(g, c, shape, k, buf[*cur], buf[*cur ^ 1], l == 0, l == nlaunch - 1,
+                             slots, i, err, tune.tz, K, nullptr, s));
     *cur ^= 1;
     done += k;
   }

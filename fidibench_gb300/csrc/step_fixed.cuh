@@ -27,6 +27,7 @@ struct FixedArgs {
   ScaleSlot* slot_out;
   ScaleSlot* slot_reset;
   int* err;
+  int* scale_log;  // nullable: block 0 records the scale of this launch's output
 };
 
 __device__ __forceinline__ int wrap_mod(int i, int n) {
@@ -328,6 +329,7 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
     a.slot_reset->kind = 1;
     a.slot_out->s = s;
     a.slot_out->kind = 1;
+    if (a.scale_log) *a.scale_log = s;
   }
   unsigned long long my_or = 0ull;
   advance_tile<K, R, W, HSM, kLoadCpAsync>(a, tile_x, tile_y, tile_z, K, IN_F64, OUT_F64, s, d,
@@ -381,6 +383,11 @@ void launch_shape(int K, bool in_f64, bool out_f64, unsigned blocks, const int64
 fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K, int tz_override,
                               int64_t resident_ctas);
 int guard_bits(const Coeffs3& c, int K);
+// One launch of the single-field kernel (K steps, explicit buffers and slot
+// ring position i); scale_log (nullable, device) receives the output scale.
+int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
+                     bool in_f64, bool out_f64, fx::ScaleSlot* slots, int i, int* err,
+                     int tz_override, int guard_K, int* scale_log, cudaStream_t st);
 namespace fx {
 
 // defined in step_fixed_<shape>.cu

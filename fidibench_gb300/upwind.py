@@ -32,6 +32,14 @@ def _as_f64(seq) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(seq, dtype=np.float64))
 
 
+def _order_after_torch(t) -> None:
+    """The library works on its own CUDA stream; a tensor torch has just
+    written on its current stream must be complete before the library reads
+    (or overwrites) it, so wait for that stream here."""
+    import torch
+    torch.cuda.current_stream(t.device).synchronize()
+
+
 class Upwind:
     """Periodic N-D first-order upwind advection of a scalar field (FP64)."""
 
@@ -159,6 +167,7 @@ class Upwind:
             t = values.detach().to(dtype=__import__("torch").float64).contiguous()
             if t.numel() != self.ntot:
                 raise ValueError(f"field has {t.numel()} values, expected {self.ntot}")
+            _order_after_torch(t)
             check(lib.fdb_upwind_set_field(self._h, t.data_ptr(), 1))
             return
         a = _as_f64(values).reshape(-1)
@@ -171,6 +180,8 @@ class Upwind:
         if out is None:
             return self.f
         is_dev = 1 if getattr(out, "is_cuda", False) else 0
+        if is_dev:
+            _order_after_torch(out)
         check(lib.fdb_upwind_get_field(self._h, _capi.dptr(out), is_dev))
         return out
 
@@ -196,6 +207,8 @@ class Upwind:
         (grad_f0, grad_v).  lambda_T/grad_f0 may be numpy arrays or CUDA
         tensors (both of the same kind)."""
         is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
+        if is_dev:
+            _order_after_torch(lambda_T)
         if grad_f0 is None:
             if is_dev:
                 import torch
@@ -205,7 +218,16 @@ class Upwind:
         if not is_dev:
             lambda_T = _as_f64(lambda_T).reshape(-1)
         gv = np.zeros(self.ndims, dtype=np.float64)
+        if not is_dev:
+            grad_f0 = np.ascontiguousarray(grad_f0, dtype=np.float64)
         check(lib.fdb_upwind_adjoint(self._h, int(numTimeSteps), float(deltaTime),
                                      _capi.dptr(lambda_T), _capi.dptr(grad_f0), gv.ctypes.data,
                                      int(checkpoint_every), is_dev))
         return grad_f0, gv
+
+    def adjoint_timings(self) -> dict:
+        """Device milliseconds of the last adjoint call, by phase."""
+        ms = np.zeros(3, dtype=np.float64)
+        check(lib.fdb_upwind_adjoint_timings(self._h, ms.ctypes.data))
+        return {"forward_ms": float(ms[0]), "recompute_ms": float(ms[1]),
+                "adjoint_ms": float(ms[2])}

@@ -139,6 +139,12 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
                        const double* lambda_T, double* grad_f0, double* grad_v,
                        int checkpoint_every, int is_device);
 
+/* Device time (ms) of the last fdb_upwind_adjoint call, by phase: ms3[0] =
+ * forward pass with checkpoints, ms3[1] = recompute of the segment states
+ * (fixed-point path; 0 for the FP64 path, whose recompute is interleaved),
+ * ms3[2] = transposed steps (in the FP64 path: recompute + transposed steps). */
+int fdb_upwind_adjoint_timings(fdb_upwind* h, double* ms3);
+
 /* One transposed step on caller buffers (device pointers):
  * lam_out = A^T lam_in, and dcoef[j] += -<lam_in, S_j f - f> (host array).
  * Used by tests and by callers that manage their own checkpoints. */

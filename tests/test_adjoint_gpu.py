@@ -62,8 +62,8 @@ def _fd_diff(fp, fm, target, h):
     return float(np.sum((rp - rm) * (rp + rm))) / (4.0 * h)
 
 
-def _forward(fdb, v, L, n, f0, steps, dt):
-    up = fdb.Upwind(v, L, n, arith="fma")
+def _forward(fdb, v, L, n, f0, steps, dt, arith="fma"):
+    up = fdb.Upwind(v, L, n, arith=arith)
     up.f = f0
     up.advect(steps, dt)
     out = up.f
@@ -71,33 +71,58 @@ def _forward(fdb, v, L, n, f0, steps, dt):
     return out
 
 
-def test_finite_differences(fdb, port):
+@pytest.mark.parametrize("arith", ["fma", "fixed"])
+def test_finite_differences(fdb, port, arith):
+    """FP64 adjoint (arith fma) and the fixed-point adjoint (arith fixed, the
+    default) against central differences of the same forward arithmetic."""
     n, L = (32, 24, 40), (1.0, 1.0, 1.0)
     v = np.array([0.8, 0.5, -0.6])
     steps, dt = 60, 0.5 / 40
     rng = np.random.default_rng(8)
     f0 = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.25, 0.01, 1)
     target = rng.standard_normal(f0.size)
-    up = fdb.Upwind(v, L, n, arith="fma")
+    up = fdb.Upwind(v, L, n, arith=arith)
     up.f = f0
     up.advect(steps, dt)
     lam = up.f - target
     up.f = f0
     g0, gv = up.adjoint(steps, dt, lam, checkpoint_every=20)
+    t = up.adjoint_timings()
+    assert t["forward_ms"] > 0 and t["adjoint_ms"] > 0
     up.close()
     h = 1e-6
     for k in range(4):
         d = rng.standard_normal(f0.size)
-        fd = _fd_diff(_forward(fdb, v, L, n, f0 + h * d, steps, dt),
-                      _forward(fdb, v, L, n, f0 - h * d, steps, dt), target, h)
+        fd = _fd_diff(_forward(fdb, v, L, n, f0 + h * d, steps, dt, arith),
+                      _forward(fdb, v, L, n, f0 - h * d, steps, dt, arith), target, h)
         assert float(g0 @ d) == pytest.approx(fd, rel=FD_TOL)
     for j in range(3):
         vp, vm = v.copy(), v.copy()
         vp[j] += h
         vm[j] -= h
-        fd = _fd_diff(_forward(fdb, vp, L, n, f0, steps, dt),
-                      _forward(fdb, vm, L, n, f0, steps, dt), target, h)
+        fd = _fd_diff(_forward(fdb, vp, L, n, f0, steps, dt, arith),
+                      _forward(fdb, vm, L, n, f0, steps, dt, arith), target, h)
         assert gv[j] == pytest.approx(fd, rel=FD_TOL)
+
+
+@pytest.mark.parametrize("v", [(1.0, -0.7, 0.3), (-0.3, -0.9, 0.6), (0.5, 0.0, -0.5)])
+def test_fixed_adjoint_matches_fp64_adjoint(fdb, v):
+    """The two adjoint arithmetics agree to ~1e-13 of max|grad|."""
+    n, L = (20, 28, 36), (1.0, 1.0, 1.0)
+    steps, dt = 45, 0.45 / 36
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(int(np.prod(n)))
+    lam = rng.standard_normal(x.size)
+    out = {}
+    for arith in ("fma", "fixed"):
+        up = fdb.Upwind(v, L, n, arith=arith)
+        up.f = x
+        out[arith] = up.adjoint(steps, dt, lam, checkpoint_every=10)
+        up.close()
+    g_fma, gv_fma = out["fma"]
+    g_fix, gv_fix = out["fixed"]
+    assert rel_maxnorm(g_fix, g_fma) <= 1e-12
+    assert np.allclose(gv_fix, gv_fma, rtol=1e-10, atol=1e-10 * np.abs(gv_fma).max())
 
 
 def test_adjoint_device_buffers(fdb):
