@@ -33,8 +33,8 @@ using fx::ScaleSlot;
 
 namespace {
 
-constexpr int kAR = 4;   // rows per thread
-constexpr int kAW = 16;  // warps per CTA
+constexpr int kAR = 4;  // rows per thread
+constexpr int kAW = 8;  // warps per CTA
 
 __device__ __forceinline__ void split_balanced(int64_t v, int32_t* hi, int32_t* lo) {
   const int32_t l = (int32_t)(uint32_t)v;
@@ -51,16 +51,33 @@ __device__ __forceinline__ int64_t prod64(int64_t D, int32_t g1, int32_t g0) {
   return fx::mad_s(d1, g1, t >> 32);
 }
 
-template <int R, int W>
+// 128-bit accumulator of signed int64 terms
+struct Acc128 {
+  unsigned long long lo = 0ull;
+  long long hi = 0ll;
+  __device__ __forceinline__ void add(int64_t v) {
+    const unsigned long long nlo = lo + (unsigned long long)v;
+    hi += (long long)(nlo < lo) + (v >> 63);
+    lo = nlo;
+  }
+  __device__ __forceinline__ double to_double() const {
+    return fma((double)hi, 18446744073709551616.0, (double)lo);
+  }
+};
+
+// One step per launch.  Every warp is independent: it owns 32 columns x R
+// rows of the logical (x, y) plane and marches along z; it loads its own
+// y-1 halo row and lane 0 loads the x-1 column, so no barrier is needed and
+// every lane computes an output.  The plane z-1 value of each cell is the
+// thread's previous-plane register.  Loads of the next plane are issued
+// into registers while the current plane is computed.
+// DOTS = false gives the plain forward step with the same structure (used to
+// recompute the forward states of a segment, one step per launch).
+template <int R, int W, bool DOTS>
 __global__ void __launch_bounds__(32 * W, 2)
 k_adjoint_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out,
                 const int64_t* __restrict__ fstate, const int* __restrict__ fscale,
                 const FixedArgs a, double* __restrict__ dpart) {
-  constexpr int K = 1;
-  constexpr int kThreads = 32 * W;
-  extern __shared__ __align__(16) int64_t s_dyn[];  // [2 buffers][lam, f][R][threads]
-  int64_t(*s_pre)[2][R][kThreads] = reinterpret_cast<int64_t(*)[2][R][kThreads]>(s_dyn);
-  __shared__ int64_t s_row[2][W][32];
   __shared__ unsigned long long s_or[W];
   __shared__ double s_red[3][W];
 
@@ -80,126 +97,123 @@ k_adjoint_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out,
     a.slot_reset->kind = 1;
     a.slot_out->s = s;
     a.slot_out->kind = 1;
+    if (a.scale_log) *a.scale_log = s;
   }
-  const int sf = *fscale;
+  const int sf = DOTS ? *fscale : 0;
 
-  const int X0 = tile_x * a.tx;
-  const int Y0 = tile_y * a.ty;
-  const int Z0 = tile_z * a.tz;
-  const int lx = fx::wrap_mod(X0 - K + lane, a.nx);
+  // logical coordinates of this thread's column and rows
+  const int gx = tile_x * 32 + lane;
+  const bool in_x = gx < a.nx;
+  const int lx = gx < a.nx ? gx : a.nx - 1;  // clamp idle lanes onto a valid column
+  const int lxm = fx::wrap_mod(lx - 1, a.nx);
   const int px = a.fx ? a.nx - 1 - lx : lx;
-  const bool out_x = (lane >= K) && (X0 + lane - K < a.nx);
-  const int ly0 = Y0 - K + warp * R;
-  const bool rows_linear = (ly0 >= 0) && (ly0 + R - 1 < a.ny);
-  const int rstep = a.fy ? -a.nx : a.nx;
-  const int roff0 =
-      (a.fy ? a.ny - 1 - fx::wrap_mod(ly0, a.ny) : fx::wrap_mod(ly0, a.ny)) * a.nx + px;
-  auto row_off = [&](int r) -> int {
-    if (rows_linear) return roff0 + r * rstep;
-    const int ly = fx::wrap_mod(ly0 + r, a.ny);
-    return (a.fy ? a.ny - 1 - ly : ly) * a.nx + px;
+  const int pxm = a.fx ? a.nx - 1 - lxm : lxm;
+  const int Y0 = tile_y * (R * W) + warp * R;
+  auto prow = [&](int ly) {  // physical row offset of logical row ly (wrapped)
+    const int w = fx::wrap_mod(ly, a.ny);
+    return (a.fy ? a.ny - 1 - w : w) * a.nx;
   };
-  const int64_t plane_sz = (int64_t)a.ny * a.nx;
-  const int nplanes = a.tz + K;
-  auto plane_off = [&](int lz) -> int64_t {
-    return (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
-  };
+  int roff[R];
   unsigned row_mask = 0u;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int ry = warp * R + r;
-    if (out_x && ry >= K && Y0 + ry - K < a.ny) row_mask |= 1u << r;
+    roff[r] = prow(Y0 + r);
+    if (in_x && Y0 + r < a.ny) row_mask |= 1u << r;
   }
+  const int rhalo = prow(Y0 - 1);
+  const int64_t plane_sz = (int64_t)a.ny * a.nx;
+  const int Z0 = tile_z * a.tz;
+  const int nz_tile = min(a.tz, a.nz - Z0);
+  auto plane_off = [&](int lz) -> int64_t {
+    return (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
+  };
 
-  int64_t hist[R];
-  int64_t cur[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) hist[r] = 0;
-  double dacc[3] = {0.0, 0.0, 0.0};
-  unsigned long long my_or = 0ull;
-
-  int lz = fx::wrap_mod(Z0 - K, a.nz);
+  // plane values: lam rows, the y-1 halo row, lane 0's x-1 column, f rows
+  int64_t cur[R], hist[R], nx_cur[R], nx_f[R], nx_xl[R], fv[R], xl[R];
+  int64_t yh, nx_yh;
+  int lz = fx::wrap_mod(Z0 - 1, a.nz);
   {
     const int64_t po = plane_off(lz);
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      fx::cp_async8(&s_pre[0][0][r][tid], in + po + row_off(r));
-      fx::cp_async8(&s_pre[0][1][r][tid], fstate + po + row_off(r));
-    }
-    fx::cp_async_commit();
+    for (int r = 0; r < R; ++r) hist[r] = __ldg(in + po + roff[r] + px);
   }
-  int parity = 0;
-  for (int p = 0; p < nplanes; ++p) {
-    const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
-    if (p + 1 < nplanes) {
-      const int64_t po = plane_off(lz_next);
+  lz = (lz + 1 == a.nz) ? 0 : lz + 1;
+  auto load_plane = [&](int z) {
+    const int64_t po = plane_off(z);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        fx::cp_async8(&s_pre[(p + 1) & 1][0][r][tid], in + po + row_off(r));
-        fx::cp_async8(&s_pre[(p + 1) & 1][1][r][tid], fstate + po + row_off(r));
-      }
+    for (int r = 0; r < R; ++r) {
+      nx_cur[r] = __ldg(in + po + roff[r] + px);
+      nx_f[r] = DOTS ? __ldg(fstate + po + roff[r] + px) : 0;
+      nx_xl[r] = (lane == 0) ? __ldg(in + po + roff[r] + pxm) : 0;
     }
-    fx::cp_async_commit();
-    fx::cp_async_wait<1>();
+    nx_yh = __ldg(in + po + rhalo + px);
+  };
+  if (nz_tile > 0) load_plane(lz);
+  if (d != 0) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) cur[r] = s_pre[p & 1][0][r][tid];
+    for (int r = 0; r < R; ++r) hist[r] = d > 0 ? (hist[r] << d) : (hist[r] >> (-d));
+  }
+
+  Acc128 acc[3];
+  unsigned long long my_or = 0ull;
+  for (int p = 0; p < nz_tile; ++p) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      cur[r] = nx_cur[r];
+      fv[r] = nx_f[r];
+      xl[r] = nx_xl[r];
+    }
+    yh = nx_yh;
+    const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
+    if (p + 1 < nz_tile) load_plane(lz_next);
     if (d != 0) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) cur[r] = d > 0 ? (cur[r] << d) : (cur[r] >> (-d));
+      for (int r = 0; r < R; ++r) {
+        cur[r] = d > 0 ? (cur[r] << d) : (cur[r] >> (-d));
+        xl[r] = d > 0 ? (xl[r] << d) : (xl[r] >> (-d));
+      }
+      yh = d > 0 ? (yh << d) : (yh >> (-d));
     }
-    const bool store = (p >= K) && (Z0 + p - K < a.nz);
-    s_row[parity][warp][lane] = cur[R - 1];
-    __syncthreads();
-    const int64_t up0 = (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0];
-    parity ^= 1;
-    int64_t left[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
     int64_t pz = 0, py = 0, pxx = 0;
+    int64_t* dst = out + plane_off(lz);
 #pragma unroll
-    for (int r = R - 1; r >= 0; --r) {
+    for (int r = 0; r < R; ++r) {
       const int64_t c = cur[r];
-      const int64_t upv = (r > 0) ? cur[r - 1] : up0;
-      const int64_t Dz = hist[r] - c, Dy = upv - c, Dx = left[r] - c;
-      const int64_t nv = fx::update(c, hist[r], upv, left[r], a);
-      if (store && (row_mask & (1u << r))) {
-        int32_t g1, g0;
-        split_balanced(s_pre[p & 1][1][r][tid], &g1, &g0);
-        pz += prod64(Dz, g1, g0);
-        py += prod64(Dy, g1, g0);
-        pxx += prod64(Dx, g1, g0);
+      int64_t left = __shfl_up_sync(0xffffffffu, c, 1);
+      if (lane == 0) left = xl[r];
+      const int64_t upv = (r > 0) ? cur[r - 1] : yh;
+      const int64_t nv = fx::update(c, hist[r], upv, left, a);
+      if (row_mask & (1u << r)) {
+        if (DOTS) {
+          int32_t g1, g0;
+          split_balanced(fv[r], &g1, &g0);
+          pz += prod64(hist[r] - c, g1, g0);
+          py += prod64(upv - c, g1, g0);
+          pxx += prod64(left - c, g1, g0);
+        }
+        my_or |= (unsigned long long)(nv ^ (nv >> 63));
+        dst[roff[r] + px] = nv;
       }
       hist[r] = c;
-      cur[r] = nv;
     }
-    if (store) {
-      dacc[0] += (double)pz;
-      dacc[1] += (double)py;
-      dacc[2] += (double)pxx;
-      int64_t* dst = out + plane_off(lz);
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        if (row_mask & (1u << r)) {
-          const int64_t v = cur[r];
-          my_or |= (unsigned long long)(v ^ (v >> 63));
-          dst[row_off(r)] = v;
-        }
-      }
-    }
+    acc[0].add(pz);
+    acc[1].add(py);
+    acc[2].add(pxx);
     lz = lz_next;
   }
-  fx::cp_async_wait<0>();
 
   // CTA sums of the three contractions, in units of 2^(64 - s - sf)
+  if (DOTS) {
 #pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    double v = dacc[j];
+    for (int j = 0; j < 3; ++j) {
+      double v = acc[j].to_double();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_red[j][warp] = v;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) s_red[j][warp] = v;
+    }
   }
   fx::cta_or<W>(my_or, s_or, &a.slot_out->m);  // contains __syncthreads
-  if (tid == 0) {
+  if (DOTS && tid == 0) {
     const double unit = ldexp(1.0, 64 - s - sf);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -314,8 +328,32 @@ size_t adjoint_fixed_scratch_bytes(int seg_len) {
   return 6 * sizeof(ScaleSlot) + 4 * sizeof(int) + (size_t)(seg_len + 1) * sizeof(int);
 }
 
+// Tiling of the warp-independent one-step kernel: 32 columns x (kAR*kAW)
+// rows per CTA, tz planes chosen for about four waves of two CTAs per SM.
+// transpose = true: the adjoint (every upwind direction reversed).
+static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
+  FixedArgs a = make_fixed_args(transpose ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
+                                (int64_t)2 * 152);
+  a.tx = 32;
+  a.ty = kAR * kAW;
+  a.tiles_x = (a.nx + a.tx - 1) / a.tx;
+  a.tiles_y = (a.ny + a.ty - 1) / a.ty;
+  const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
+  const int64_t want = 4 * 2 * 152;
+  int64_t cz = (want + txy - 1) / txy;
+  if (cz < 1) cz = 1;
+  int tz = (int)((a.nz + cz - 1) / cz);
+  if (tz < 4) tz = 4;
+  if (tz > a.nz) tz = a.nz;
+  a.tz = tz;
+  a.tiles_z = (a.nz + tz - 1) / tz;
+  a.guard = guard_bits(c, 1);
+  a.scale_log = nullptr;
+  return a;
+}
+
 int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c) {
-  const FixedArgs a = make_fixed_args(transposed(g), c, fx::kR4W16, 1, 0, (int64_t)2 * 152);
+  const FixedArgs a = step1_args(g, c, true);
   return a.tiles_x * a.tiles_y * a.tiles_z;
 }
 
@@ -328,21 +366,10 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   int* err = (int*)(fr + 6);
   int* logs = err + 4;                      // scale of each recomputed state
   const int gK = guard_bits(c, 1);
-  const int shape = fx::kR4W16;
-  const Geom gT = transposed(g);
-
-  // adjoint kernel shape and its dynamic shared memory
-  constexpr int smem = 2 * 2 * kAR * 32 * kAW * (int)sizeof(int64_t);
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_adjoint_fixed<kAR, kAW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         smem);
-    configured = true;
-  }
-  FixedArgs aT = make_fixed_args(gT, c, shape, 1, 0, (int64_t)2 * 152);
-  aT.guard = gK;
+  FixedArgs aT = step1_args(g, c, true);
   aT.err = err;
-  aT.scale_log = nullptr;
+  FixedArgs aF = step1_args(g, c, false);
+  aF.err = err;
   const int nblk = aT.tiles_x * aT.tiles_y * aT.tiles_z;
   if (nblk > io.dpart_cap) return fail(FDB_ERR_INVALID, "adjoint partial-sum buffer too small");
 
@@ -370,9 +397,16 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
     k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.states[0], n, fr, fr + 1, fr + 2, gK,
                                            logs + 0, err);
     note_launch(3);
-    for (int k = 1; k < len; ++k)
-      FDB_TRY(launch_fixed_one(g, c, shape, 1, io.states[k - 1], io.states[k], false, false, fr, k,
-                               err, 0, 1, logs + k, st));
+    for (int k = 1; k < len; ++k) {
+      aF.slot_in = fr + (k % 3);
+      aF.slot_out = fr + ((k + 1) % 3);
+      aF.slot_reset = fr + ((k + 2) % 3);
+      aF.scale_log = logs + k;
+      k_adjoint_fixed<kAR, kAW, false><<<nblk, 32 * kAW, 0, st>>>(
+          io.states[k - 1], io.states[k], nullptr, nullptr, aF, nullptr);
+      note_launch();
+    }
+    FDB_CUDA_TRY(cudaGetLastError());
     if (io.recompute_ev) {
       cudaEventRecord(e1, st);
       io.recompute_ev->push_back({e0, e1});
@@ -382,7 +416,7 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aT.slot_in = lr + (li % 3);
       aT.slot_out = lr + ((li + 1) % 3);
       aT.slot_reset = lr + ((li + 2) % 3);
-      k_adjoint_fixed<kAR, kAW><<<nblk, 32 * kAW, smem, st>>>(io.lam[lc], io.lam[lc ^ 1],
+      k_adjoint_fixed<kAR, kAW, true><<<nblk, 32 * kAW, 0, st>>>(io.lam[lc], io.lam[lc ^ 1],
                                                                io.states[k], logs + k, aT,
                                                                io.dpart);
       note_launch();
