@@ -391,6 +391,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-looped leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-recovery", action="store_true",
+                    help="skip the batched adjoint (gradient-descent recovery) leg")
     ap.add_argument("--n", type=int, default=512, help="cube size (profiling only)")
     ap.add_argument("--tz", type=int, default=0, help="fixed kernel z-tile override")
     ap.add_argument("--shape", type=int, default=-1, help="fixed kernel CTA shape (0..2)")
@@ -497,6 +499,12 @@ def main() -> None:
     adjoint = None
     if not args.no_adjoint:
         adjoint = bench_adjoint(stream)
+    recovery = None
+    if not args.no_recovery:
+        # batched adjoint: 64 instances of 128^3, seeded velocities in [-1,1]^3,
+        # 100 steps, 20 gradient-descent iterations through the autograd Function
+        from fidibench_gb300.recovery import recover
+        recovery = recover(count=64, n=128, steps=100, iters=20, seed=SEED)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -526,6 +534,7 @@ def main() -> None:
             "gpu_launches": launches,
             "batched": batched,
             "adjoint": adjoint,
+            "batched_adjoint_recovery": recovery,
         }
         print(json.dumps(line))
     if dist is not None:
