@@ -182,27 +182,34 @@ BATCH_STEPS = 50
 BATCH_SEED = 20261203
 
 
-def bench_batched(steps: int, warmup: int, stream) -> dict:
+def bench_batched(steps: int, warmup: int, stream, rank: int = 0, ws: int = 1) -> dict:
     """Batched form: 256 independent 3-D FP64 problems, axes uniform in
     [32, 160], velocities uniform in [-1, 1]^3, CFL 0.5, 50 steps, sphere
     initial fields (seeded centres/radii).  One persistent launch per advect
     (replayed from a CUDA graph), tuned by the library's autotuner, against
-    the single-field kernel looped over the same instances."""
+    the single-field kernel looped over the same instances.  With N ranks the
+    instances are split by a size-balanced partition (no exchange during the
+    advect); rates use the slowest rank's time."""
     import torch
     import fidibench_gb300 as fdb
     from fidibench_gb300.batch import random_instances
+    from fidibench_gb300.sharding import gather_by_index, partition_instances, reduce_max
 
-    specs = random_instances(BATCH_COUNT, BATCH_SEED)
+    all_specs = random_instances(BATCH_COUNT, BATCH_SEED)
+    sizes = [int(np.prod(s["n"])) for s in all_specs]
+    mine = partition_instances(sizes, ws)[rank]
+    specs = [all_specs[i] for i in mine]
     b = fdb.Batch([(s["v"], s["L"], s["n"]) for s in specs])
     b.set_stream(stream)
     dts = [s["dt"] for s in specs]
 
     def reset():
-        for k, s in enumerate(specs):
-            b.init_sphere(k, s["center"], s["radius"], 0.0, BATCH_SEED + k)
+        for k, i in enumerate(mine):
+            s = all_specs[i]
+            b.init_sphere(k, s["center"], s["radius"], 0.0, BATCH_SEED + i)
 
     reset()
-    cells = float(b.total_cells)
+    cells = float(sum(sizes))
     t0 = time.perf_counter()
     chosen = b.autotune(BATCH_STEPS, dts)
     tune_s = time.perf_counter() - t0
@@ -218,21 +225,21 @@ def bench_batched(steps: int, warmup: int, stream) -> dict:
             fn()
         e1.record(stream)
         e1.synchronize()
-        return e0.elapsed_time(e1) / steps
+        return reduce_max(e0.elapsed_time(e1) / steps)
 
     reset()
     ms_batched = timed(lambda: b.advect(BATCH_STEPS, dts))
-    sums_batched = b.checksums()
+    sums_batched = gather_by_index(dict(zip(mine, b.checksums())), BATCH_COUNT)
     reset()
     ms_looped = timed(lambda: b.advect_looped(BATCH_STEPS, dts))
-    sums_looped = b.checksums()
+    sums_looped = gather_by_index(dict(zip(mine, b.checksums())), BATCH_COUNT)
     b.close()
     gb = cells * BATCH_STEPS / (ms_batched * 1e-3) / 1e9
     gl = cells * BATCH_STEPS / (ms_looped * 1e-3) / 1e9
     agree = float(np.max(np.abs(sums_batched - sums_looped) / np.maximum(np.abs(sums_looped), 1e-300)))
     return {"workload": f"batch{BATCH_COUNT}_uneven32-160_{BATCH_STEPS}steps",
             "instances": BATCH_COUNT, "cells": int(cells), "time_steps": BATCH_STEPS,
-            "batched_gcups": gb, "looped_gcups": gl, "ratio": gb / gl,
+            "ranks": ws, "batched_gcups": gb, "looped_gcups": gl, "ratio": gb / gl,
             "ms_per_advect_batched": ms_batched, "ms_per_advect_looped": ms_looped,
             "tuning": chosen, "autotune_s": tune_s, "graph_replay": True,
             "checksum_rel_diff_batched_vs_looped": agree}
@@ -495,12 +502,13 @@ def main() -> None:
 
     batched = None
     if not args.no_batch:
-        batched = bench_batched(max(3, min(args.steps, 5)), 3, stream)
+        batched = bench_batched(max(3, min(args.steps, 5)), 3, stream, rank, ws)
+    # the adjoint and recovery legs are single-GPU workloads: rank 0 runs them
     adjoint = None
-    if not args.no_adjoint:
+    if not args.no_adjoint and rank == 0:
         adjoint = bench_adjoint(stream)
     recovery = None
-    if not args.no_recovery:
+    if not args.no_recovery and rank == 0:
         # batched adjoint: 64 instances of 128^3, seeded velocities in [-1,1]^3,
         # 100 steps, 20 gradient-descent iterations through the autograd Function
         from fidibench_gb300.recovery import recover
