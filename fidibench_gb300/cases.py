@@ -1,0 +1,55 @@
+"""Small stand-alone runs of one kernel family, for profiling a single launch
+on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
+
+  adjoint N S : N^3 field, v = (0.8, 0.5, -0.6), dt = 0.5 min(dx/|v|), three
+                adjoint calls of S steps with one checkpoint segment
+  advect N S  : N^3 sphere + noise field, v = (1, -0.7, 0.3), dt = 0.5/N,
+                three advect calls of S steps
+"""
+from __future__ import annotations
+
+import sys
+
+
+def adjoint_case(n: int, steps: int) -> dict:
+    import torch
+    import fidibench_gb300 as fdb
+    v = (0.8, 0.5, -0.6)
+    dt = 0.5 * min(1.0 / n / abs(x) for x in v)
+    up = fdb.Upwind(v, (1.0,) * 3, (n,) * 3)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1)
+    lam = torch.randn(n ** 3, device="cuda", dtype=torch.float64, generator=gen)
+    for _ in range(3):
+        up.init_sphere((0.5,) * 3, 0.2, 0.01, 1)
+        up.adjoint(steps, dt, lam, checkpoint_every=steps)
+    t = up.adjoint_timings()
+    up.close()
+    return t
+
+
+def advect_case(n: int, steps: int) -> float:
+    import fidibench_gb300 as fdb
+    up = fdb.Upwind((1.0, -0.7, 0.3), (1.0,) * 3, (n,) * 3)
+    up.init_sphere((0.5,) * 3, 0.2, 0.01, 1)
+    for _ in range(3):
+        up.advect(steps, 0.5 / n)
+    cs = up.checksum()
+    up.close()
+    return cs
+
+
+def main(argv: list[str]) -> int:
+    if len(argv) != 3 or argv[0] not in ("adjoint", "advect"):
+        print(__doc__)
+        return 2
+    n, steps = int(argv[1]), int(argv[2])
+    if argv[0] == "adjoint":
+        print(adjoint_case(n, steps))
+    else:
+        print(advect_case(n, steps))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))

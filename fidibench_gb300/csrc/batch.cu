@@ -122,9 +122,10 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
     const int64_t* in = ((b & 1) ? arena1 : arena0) + I.offset;
     int64_t* out = ((b & 1) ? arena0 : arena1) + I.offset;
     unsigned long long my_or = 0ull;
-    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(I.a, tx, ty, tz, levels, b == 0,
-                                                     b == nblocks - 1, s, d, in, out, s_dyn,
-                                                     s_row, my_or);
+    const int z0 = tz * I.a.tz;
+    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(I.a, tx, ty, z0, min(I.a.tz, I.a.nz - z0),
+                                                     levels, b == 0, b == nblocks - 1, s, d, in,
+                                                     out, s_dyn, s_row, my_or);
     fx::cta_or<W>(my_or, s_or, &sl[(b + 1) % 3].m);
     __threadfence();
     __syncthreads();

@@ -137,6 +137,40 @@ fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K,
   return a;
 }
 
+namespace fx {
+
+long long plan_slabs(FixedArgs& a, int resident, int cap) {
+  const long long txy = (long long)a.tiles_x * a.tiles_y;
+  const int nz = a.nz;
+  if (txy <= 0 || nz <= 0) {
+    a.nslab = 0;
+    return 0;
+  }
+  const long long res = resident > 0 ? resident : 1;
+  int h0 = cap;
+  if (h0 <= 0) {
+    h0 = (int)((txy * nz + 4 * res - 1) / (4 * res));
+    if (h0 < 32) h0 = 32;
+  }
+  if (h0 > nz) h0 = nz;
+  const int hmin = h0 < 8 ? h0 : 8;
+  int z = 0, i = 0;
+  while (z < nz) {
+    const int rem = nz - z;
+    long long h = (txy * rem + res - 1) / res;  // remaining planes per resident CTA
+    if (h > h0) h = h0;
+    if (h < hmin) h = hmin;
+    if (h > rem || i == kMaxSlabs - 1) h = rem;
+    a.slab_z[i++] = z;
+    z += (int)h;
+  }
+  a.slab_z[i] = nz;
+  a.nslab = i;
+  return txy * i;
+}
+
+}  // namespace fx
+
 int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
                      bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err,
                      int tz_override, int guard_K, int* scale_log, cudaStream_t st) {
@@ -152,17 +186,18 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
   a.slot_reset = slots + ((i + 2) % 3);
   a.err = err;
   a.scale_log = scale_log;
-  const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
-  const int64_t blocks = txy * a.tiles_z;
-  if (blocks > 0x7FFFFFFF) return fail(FDB_ERR_UNSUPPORTED, "grid too large for the fixed kernel");
+  // the grid is at most tiles_x * tiles_y * kMaxSlabs CTAs
+  if ((int64_t)a.tiles_x * a.tiles_y * fx::kMaxSlabs > 0x7FFFFFFF)
+    return fail(FDB_ERR_UNSUPPORTED, "grid too large for the fixed kernel");
   const int64_t* pin = (const int64_t*)in;
   int64_t* pout = (int64_t*)out;
+  const int cap = tz_override > 0 ? tz_override : 0;
   switch (shape) {
-    case fx::kR4W16: fx::launch_r4w16(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
-    case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
-    case fx::kR4W16S: fx::launch_r4w16s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
-    case fx::kR4W8S: fx::launch_r4w8s(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
-    default: fx::launch_r8w8(K, in_f64, out_f64, (unsigned)blocks, pin, pout, a, st); break;
+    case fx::kR4W16: fx::launch_r4w16(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    case fx::kR4W16S: fx::launch_r4w16s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    case fx::kR4W8S: fx::launch_r4w8s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    default: fx::launch_r8w8(K, in_f64, out_f64, cap, pin, pout, a, st); break;
   }
   note_launch();
   FDB_CUDA_TRY(cudaGetLastError());

@@ -16,11 +16,17 @@ struct ScaleSlot {
   int kind;
 };
 
+constexpr int kMaxSlabs = 24;
+
 struct FixedArgs {
   int nz, ny, nx;
   int fz, fy, fx;  // 1: physical axis reversed relative to the logical one
   int tx, ty, tz;
   int tiles_x, tiles_y, tiles_z;
+  // k_advect_fixed: z-slabs [slab_z[i], slab_z[i+1]), i < nslab, one CTA per
+  // (slab, tile); the other kernels tile z uniformly by tz
+  int nslab;
+  int slab_z[kMaxSlabs + 1];
   QCoeff qz, qy, qx;
   int guard;
   const ScaleSlot* slot_in;
@@ -124,13 +130,13 @@ __device__ __forceinline__ bool scale_from_slot(const ScaleSlot* slot, int guard
 enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1 };
 
 // Advance one tile of one field by `levels` (<= K) steps.  The tile's output
-// region is x in [X0, X0+tx), y in [Y0, Y0+ty), z in [Z0, Z0+tz) of the
-// logical axes; the CTA computes a (32) x (R*W) x (tz+K) region that starts
-// K cells upstream on every axis.  my_or accumulates |F| bits of the stored
+// region is x in [X0, X0+tx), y in [Y0, Y0+ty), z in [Z0, Z0+nout) of the
+// logical axes (Z0 + nout <= nz); the CTA computes a (32) x (R*W) x (nout+K)
+// region that starts K cells upstream on every axis.  my_or accumulates |F| bits of the stored
 // outputs.  Callers synchronise the CTA before reusing shared memory.
 template <int K, int R, int W, bool HSM, int LOADER>
-__device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int tile_z,
-                                             int levels, bool in_f64, bool out_f64, int s, int d,
+__device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int Z0,
+                                             int nout, int levels, bool in_f64, bool out_f64, int s, int d,
                                              const int64_t* __restrict__ in,
                                              int64_t* __restrict__ out, int64_t* s_dyn,
                                              int64_t (*s_row)[W][32],
@@ -145,7 +151,6 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   const int warp = tid >> 5;
   const int X0 = tile_x * a.tx;
   const int Y0 = tile_y * a.ty;
-  const int Z0 = tile_z * a.tz;
 
   const int lx = wrap_mod(X0 - K + lane, a.nx);
   const int px = a.fx ? a.nx - 1 - lx : lx;
@@ -163,7 +168,7 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
     return (a.fy ? a.ny - 1 - ly : ly) * a.nx + px;
   };
   const int64_t plane_sz = (int64_t)a.ny * a.nx;
-  const int nplanes = a.tz + K;
+  const int nplanes = nout + K;
   auto plane_ptr = [&](const int64_t* base, int lz) {
     return base + (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
   };
@@ -270,7 +275,7 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
         cur[r] = nv;
       }
     }
-    if (p >= K && Z0 + p - K < a.nz) {
+    if (p >= K) {
       int64_t* dst = const_cast<int64_t*>(plane_ptr(out, lz));
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -308,7 +313,11 @@ __device__ __forceinline__ void cta_or(unsigned long long my_or, unsigned long l
   }
 }
 
-// One launch = K steps of one field; one tile per CTA.
+// One launch = K steps of one field.  CTA b works on tile b % (tiles_x *
+// tiles_y) of z-slab b / (tiles_x * tiles_y): the CTAs that run together share
+// their halo rows through L2, and the slabs shrink towards the end of the
+// grid so that the last wave is short (the scheduler hands out CTAs in
+// index order).
 template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64>
 __global__ void __launch_bounds__(32 * W, MINB)
 k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
@@ -316,11 +325,11 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
   __shared__ int64_t s_row[2][W][32];
   __shared__ unsigned long long s_or[W];
 
-  int bid = blockIdx.x;
-  const int tile_x = bid % a.tiles_x;
-  bid /= a.tiles_x;
-  const int tile_y = bid % a.tiles_y;
-  const int tile_z = bid / a.tiles_y;
+  const int txy = a.tiles_x * a.tiles_y;
+  const int slab = (int)blockIdx.x / txy;
+  const int tile = (int)blockIdx.x - slab * txy;
+  const int z0 = a.slab_z[slab];
+  const int nout = a.slab_z[slab + 1] - z0;
 
   int s, d;
   if (!scale_from_slot(a.slot_in, a.guard, &s, &d) && threadIdx.x == 0) atomicOr(a.err, 1);
@@ -332,8 +341,8 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
     if (a.scale_log) *a.scale_log = s;
   }
   unsigned long long my_or = 0ull;
-  advance_tile<K, R, W, HSM, kLoadCpAsync>(a, tile_x, tile_y, tile_z, K, IN_F64, OUT_F64, s, d,
-                                           in, out, s_dyn, s_row, my_or);
+  advance_tile<K, R, W, HSM, kLoadCpAsync>(a, tile % a.tiles_x, tile / a.tiles_x, z0, nout, K,
+                                           IN_F64, OUT_F64, s, d, in, out, s_dyn, s_row, my_or);
   cta_or<W>(my_or, s_or, &a.slot_out->m);
 }
 
@@ -345,36 +354,50 @@ constexpr int shape_warps(int sh) {
   return (sh == kR8W8 || sh == kR8W8S || sh == kR4W8S) ? 8 : 16;
 }
 
+// z-slabs of one k_advect_fixed launch for `resident` CTAs on the GPU at once:
+// slabs of h0 planes (cap if > 0, else about a quarter of the planes per
+// resident CTA, at least 32), then slabs that follow the remaining planes per
+// resident CTA down to 8.  Sets a.nslab / a.slab_z; returns the CTA count.
+long long plan_slabs(FixedArgs& a, int resident, int cap);
+
 template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT>
-void launch_k(unsigned blocks, const int64_t* in, int64_t* out, const FixedArgs& a,
-              cudaStream_t st) {
+void launch_k(int cap, const int64_t* in, int64_t* out, FixedArgs a, cudaStream_t st) {
   constexpr int smem = fixed_smem_bytes<K, R, W, HSM>();
-  static bool configured = false;  // per instantiation; benign race (idempotent)
-  if (!configured) {
+  static int per_sm = -1;  // per instantiation; benign race (idempotent)
+  if (per_sm < 0) {
     cudaFuncSetAttribute(k_advect_fixed<K, R, W, HSM, MINB, IN, OUT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    configured = true;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ, k_advect_fixed<K, R, W, HSM, MINB, IN, OUT>, 32 * W, smem) != cudaSuccess)
+      occ = 1;
+    per_sm = occ > 0 ? occ : 1;
   }
-  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT><<<blocks, 32 * W, smem, st>>>(in, out, a);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long blocks = plan_slabs(a, per_sm * (sms > 0 ? sms : 1), cap);
+  if (blocks <= 0) return;
+  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT><<<(unsigned)blocks, 32 * W, smem, st>>>(in, out, a);
 }
 
 template <int K, int R, int W, bool HSM, int MINB>
-void launch_io(bool in_f64, bool out_f64, unsigned blocks, const int64_t* in, int64_t* out,
+void launch_io(bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,
                const FixedArgs& a, cudaStream_t st) {
-  if (in_f64 && out_f64) launch_k<K, R, W, HSM, MINB, true, true>(blocks, in, out, a, st);
-  else if (in_f64) launch_k<K, R, W, HSM, MINB, true, false>(blocks, in, out, a, st);
-  else if (out_f64) launch_k<K, R, W, HSM, MINB, false, true>(blocks, in, out, a, st);
-  else launch_k<K, R, W, HSM, MINB, false, false>(blocks, in, out, a, st);
+  if (in_f64 && out_f64) launch_k<K, R, W, HSM, MINB, true, true>(cap, in, out, a, st);
+  else if (in_f64) launch_k<K, R, W, HSM, MINB, true, false>(cap, in, out, a, st);
+  else if (out_f64) launch_k<K, R, W, HSM, MINB, false, true>(cap, in, out, a, st);
+  else launch_k<K, R, W, HSM, MINB, false, false>(cap, in, out, a, st);
 }
 
 template <int R, int W, bool HSM, int MINB>
-void launch_shape(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
-                  int64_t* out, const FixedArgs& a, cudaStream_t st) {
+void launch_shape(int K, bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,
+                  const FixedArgs& a, cudaStream_t st) {
   switch (K) {
-    case 1: launch_io<1, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    case 2: launch_io<2, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    case 3: launch_io<3, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
-    default: launch_io<4, R, W, HSM, MINB>(in_f64, out_f64, blocks, in, out, a, st); break;
+    case 1: launch_io<1, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
+    case 2: launch_io<2, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
+    case 3: launch_io<3, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
+    default: launch_io<4, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
   }
 }
 
@@ -390,10 +413,10 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
                      int tz_override, int guard_K, int* scale_log, cudaStream_t st);
 namespace fx {
 
-// defined in step_fixed_<shape>.cu
+// defined in step_fixed_<shape>.cu; cap as in plan_slabs
 #define FDB_FX_DECLARE(NAME)                                                               \
-  void NAME(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,          \
-            int64_t* out, const FixedArgs& a, cudaStream_t st);
+  void NAME(int K, bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,    \
+            const FixedArgs& a, cudaStream_t st);
 FDB_FX_DECLARE(launch_r8w8)
 FDB_FX_DECLARE(launch_r4w16)
 FDB_FX_DECLARE(launch_r8w8s)

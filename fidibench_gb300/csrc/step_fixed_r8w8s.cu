@@ -6,9 +6,9 @@
 namespace fdb {
 namespace fx {
 
-void launch_r8w8s(int K, bool in_f64, bool out_f64, unsigned blocks, const int64_t* in,
+void launch_r8w8s(int K, bool in_f64, bool out_f64, int cap, const int64_t* in,
                  int64_t* out, const FixedArgs& a, cudaStream_t st) {
-  launch_shape<8, 8, true, 2>(K, in_f64, out_f64, blocks, in, out, a, st);
+  launch_shape<8, 8, true, 2>(K, in_f64, out_f64, cap, in, out, a, st);
 }
 
 }  // namespace fx

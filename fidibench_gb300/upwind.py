@@ -85,7 +85,8 @@ class Upwind:
         check(lib.fdb_upwind_set_arith(self._h, code, int(depth)))
 
     def set_tile_z(self, tile_z: int) -> None:
-        """Output planes per CTA of the fixed-point kernel (0 = automatic)."""
+        """Most output planes one CTA of the fixed-point kernel takes along
+        the slowest axis (0 = automatic: an equal share per resident CTA)."""
         check(lib.fdb_upwind_set_tuning(self._h, 1, int(tile_z)))
 
     def set_shape(self, shape: int) -> None:

@@ -129,6 +129,29 @@ def test_step_counts_fixed_blocking(fdb, port, steps):
     assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL)
 
 
+@pytest.mark.parametrize("shape", [3, 4, 0])
+@pytest.mark.parametrize("tile_z", [0, 1, 3, 17])
+@pytest.mark.parametrize("n", [(37, 70, 45), (64, 64, 64), (9, 130, 33)])
+def test_z_run_split_vs_oracle(fdb, port, n, tile_z, shape):
+    """The fixed kernel's (tile, plane) split: runs that start at any plane,
+    cross from one tile to the next, and are capped at a few planes."""
+    v = (0.45, -0.8, 0.6)
+    L = (1.0, 1.0, 1.0)
+    rng = np.random.default_rng(n[0] * 1000 + tile_z)
+    f0 = rng.standard_normal(int(np.prod(n)))
+    dt = 0.3 * min(Lj / nj for Lj, nj in zip(L, n))
+    ref = port.advect(n, v, L, f0, 10, dt)
+    up = fdb.Upwind(v, L, n, arith="fixed")
+    up.set_tile_z(tile_z)
+    up.set_shape(shape)
+    up.f = f0
+    up.advect(10, dt)
+    out = up.f
+    assert up.arith_used == "fixed"
+    up.close()
+    assert rel_maxnorm(out, ref) <= FIELD_TOL
+
+
 def test_sphere_init_bit_exact(fdb, port):
     g = load_golden("synth_sphere_16x12x10")
     n = [int(x) for x in g["n"]]
