@@ -7,13 +7,14 @@
 // (a_j = -c_j are the Courant numbers; the second line follows from
 // <lam', S_j f - f> and the periodic shift invariance, so f is read only at
 // i).  The lam update is the forward fixed-point update with every axis
-// flipped, so the kernel reuses its tile geometry, update and scale ring
-// (step_fixed.cuh) with one step per launch: 24 B of HBM per cell-step
-// (lam in and out, f^n in).  The contraction D_j * F^n is an exact 64x64
-// product rounded to 2^64 units (three IMAD.WIDE on balanced 32-bit halves),
-// summed per thread in int64 per plane and in FP64 across planes; each CTA
-// adds its three sums into its own slot of a per-call array (fixed
-// CTA -> tile map, so the result is deterministic).
+// flipped, so the kernel reuses its update and scale ring (step_fixed.cuh)
+// with one step per launch: 24 B of HBM per cell-step (lam in and out, f^n
+// in), the differences D_j shared between the update and the contraction.
+// The contraction D_j * F^n is a 64x64 product rounded to 2^64 units (three
+// IMAD.WIDE on balanced 32-bit halves), summed per thread in int64 per plane
+// and in a 128-bit integer across planes; each CTA adds its three sums into
+// its own slot of a per-call array (fixed CTA -> tile map, so the result is
+// deterministic).
 //
 // Forward states f^n of a checkpoint segment are recomputed by the forward
 // fixed kernel with one step per launch into int64 buffers; each launch logs
@@ -22,6 +23,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "step_fixed.cuh"
@@ -36,19 +38,19 @@ namespace {
 constexpr int kAR = 4;  // rows per thread
 constexpr int kAW = 8;  // warps per CTA
 
+// v = hi 2^32 + lo with both halves signed (lo in [-2^31, 2^31))
 __device__ __forceinline__ void split_balanced(int64_t v, int32_t* hi, int32_t* lo) {
-  const int32_t l = (int32_t)(uint32_t)v;
-  *lo = l;
-  *hi = (int32_t)((v - (int64_t)l) >> 32);
+  *lo = (int32_t)(uint32_t)v;
+  *hi = (int32_t)(v >> 32) + (int32_t)((uint32_t)v >> 31);
 }
 
-// round(D * F / 2^64) from balanced halves (|D| < 2^62, |F| < 2^61)
+// round(D * F / 2^64) from balanced halves (|D| < 2^62, |F| < 2^61): the two
+// cross products (|.| <= 2^61 and 2^60) sum exactly in int64
 __device__ __forceinline__ int64_t prod64(int64_t D, int32_t g1, int32_t g0) {
   int32_t d1, d0;
   split_balanced(D, &d1, &d0);
-  int64_t t = fx::mad_s(d1, g0, 0x80000000ll);
-  t = fx::mad_s(d0, g1, t);
-  return fx::mad_s(d1, g1, t >> 32);
+  const int64_t t = mulw_s(d1, g0) + mulw_s(d0, g1) + 0x80000000ll;
+  return mulw_s(d1, g1) + (t >> 32);
 }
 
 // 128-bit accumulator of signed int64 terms
@@ -60,26 +62,62 @@ struct Acc128 {
     hi += (long long)(nlo < lo) + (v >> 63);
     lo = nlo;
   }
+  __device__ __forceinline__ void add(const Acc128& o) {
+    const unsigned long long nlo = lo + o.lo;
+    hi += o.hi + (long long)(nlo < lo);
+    lo = nlo;
+  }
+  // sum over the warp (integer shuffles), valid in every lane
+  __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      Acc128 t;
+      t.lo = __shfl_xor_sync(0xffffffffu, lo, o);
+      t.hi = __shfl_xor_sync(0xffffffffu, hi, o);
+      add(t);
+    }
+  }
   __device__ __forceinline__ double to_double() const {
     return fma((double)hi, 18446744073709551616.0, (double)lo);
   }
 };
 
-// One step per launch.  Every warp is independent: it owns 32 columns x R
-// rows of the logical (x, y) plane and marches along z; it loads its own
-// y-1 halo row and lane 0 loads the x-1 column, so no barrier is needed and
-// every lane computes an output.  The plane z-1 value of each cell is the
-// thread's previous-plane register.  Loads of the next plane are issued
-// into registers while the current plane is computed.
-// DOTS = false gives the plain forward step with the same structure (used to
-// recompute the forward states of a segment, one step per launch).
+// 2^e as a double from its bit pattern (0 below the normal range)
+__device__ __forceinline__ double pow2(int e) {
+  if (e < -1022) return 0.0;
+  if (e > 1023) e = 1024;  // infinity
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// One step per launch, one 32 x 32 (x, y) tile per CTA marching along z.
+// Each plane of the input is staged by cp.async into shared memory with its
+// upstream halo (row 0 = the y-1 row, column 0 = the x-1 column), so every
+// neighbour of a cell is one shared-memory load: no shuffles, no selects,
+// one __syncthreads per plane.  Three input planes rotate (z-1, z, and the
+// one being fetched); the forward state F^n (DOTS) is staged the same way.
+// Thread (warp w, lane l) owns cells (x = l, y = w*R + r) of the tile.
 template <int R, int W, bool DOTS>
-__global__ void __launch_bounds__(32 * W, 2)
-k_adjoint_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out,
-                const int64_t* __restrict__ fstate, const int* __restrict__ fscale,
-                const FixedArgs a, double* __restrict__ dpart) {
+struct AdjTileSmem {
+  static constexpr int kRows = R * W;              // tile rows (32)
+  static constexpr int kLRow = 33;                 // halo column + 32 cells
+  static constexpr int kLPlane = (kRows + 1) * kLRow;
+  static constexpr int kFPlane = kRows * 32;
+  static constexpr int bytes() { return (3 * kLPlane + (DOTS ? 2 * kFPlane : 0)) * 8; }
+};
+
+template <int R, int W, bool DOTS>
+__global__ void __launch_bounds__(32 * W, 3)
+k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
+               const int64_t* __restrict__ fstate, const int* __restrict__ fscale,
+               const FixedArgs a, double* __restrict__ dpart) {
+  using SM = AdjTileSmem<R, W, DOTS>;
+  static_assert(SM::kRows == 32, "the halo column is loaded by one warp");
+  extern __shared__ __align__(16) int64_t s_dyn[];
   __shared__ unsigned long long s_or[W];
-  __shared__ double s_red[3][W];
+  __shared__ unsigned long long s_red_lo[3][W];
+  __shared__ long long s_red_hi[3][W];
+  int64_t* sL = s_dyn;                  // [3][kRows + 1][33]
+  int64_t* sF = s_dyn + 3 * SM::kLPlane;  // [2][kRows][32]
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -101,15 +139,15 @@ k_adjoint_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out,
   }
   const int sf = DOTS ? *fscale : 0;
 
-  // logical coordinates of this thread's column and rows
+  // logical -> physical column and row offsets (periodic wrap, axis flips)
   const int gx = tile_x * 32 + lane;
   const bool in_x = gx < a.nx;
-  const int lx = gx < a.nx ? gx : a.nx - 1;  // clamp idle lanes onto a valid column
-  const int lxm = fx::wrap_mod(lx - 1, a.nx);
+  const int lx = in_x ? gx : a.nx - 1;  // idle lanes read a valid column
   const int px = a.fx ? a.nx - 1 - lx : lx;
+  const int lxm = fx::wrap_mod(tile_x * 32 - 1, a.nx);
   const int pxm = a.fx ? a.nx - 1 - lxm : lxm;
-  const int Y0 = tile_y * (R * W) + warp * R;
-  auto prow = [&](int ly) {  // physical row offset of logical row ly (wrapped)
+  const int Y0 = tile_y * SM::kRows;
+  auto prow = [&](int ly) {
     const int w = fx::wrap_mod(ly, a.ny);
     return (a.fy ? a.ny - 1 - w : w) * a.nx;
   };
@@ -117,110 +155,146 @@ k_adjoint_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out,
   unsigned row_mask = 0u;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    roff[r] = prow(Y0 + r);
-    if (in_x && Y0 + r < a.ny) row_mask |= 1u << r;
+    const int ly = Y0 + warp * R + r;
+    roff[r] = prow(ly);
+    if (in_x && ly < a.ny) row_mask |= 1u << r;
   }
-  const int rhalo = prow(Y0 - 1);
+  // warp 0 also fetches the y-1 row (its lanes' columns) and the x-1 column
+  // (lane l: tile row l)
+  const int rhalo = prow(Y0 - 1) + px;
+  const int chalo = prow(Y0 + lane) + pxm;
   const int64_t plane_sz = (int64_t)a.ny * a.nx;
   const int Z0 = tile_z * a.tz;
   const int nz_tile = min(a.tz, a.nz - Z0);
   auto plane_off = [&](int lz) -> int64_t {
     return (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
   };
-
-  // plane values: lam rows, the y-1 halo row, lane 0's x-1 column, f rows
-  int64_t cur[R], hist[R], nx_cur[R], nx_f[R], nx_xl[R], fv[R], xl[R];
-  int64_t yh, nx_yh;
-  int lz = fx::wrap_mod(Z0 - 1, a.nz);
-  {
-    const int64_t po = plane_off(lz);
-#pragma unroll
-    for (int r = 0; r < R; ++r) hist[r] = __ldg(in + po + roff[r] + px);
-  }
-  lz = (lz + 1 == a.nz) ? 0 : lz + 1;
-  auto load_plane = [&](int z) {
-    const int64_t po = plane_off(z);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      nx_cur[r] = __ldg(in + po + roff[r] + px);
-      nx_f[r] = DOTS ? __ldg(fstate + po + roff[r] + px) : 0;
-      nx_xl[r] = (lane == 0) ? __ldg(in + po + roff[r] + pxm) : 0;
-    }
-    nx_yh = __ldg(in + po + rhalo + px);
+  auto lam_at = [&](int buf, int row, int col) -> int64_t* {
+    return sL + buf * SM::kLPlane + row * SM::kLRow + col;
   };
-  if (nz_tile > 0) load_plane(lz);
-  if (d != 0) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) hist[r] = d > 0 ? (hist[r] << d) : (hist[r] >> (-d));
-  }
 
+  // fetch plane j (j = 0: z = Z0-1, the z-1 history of the first plane)
+  // fetch a plane (physical offset po) into lambda buffer b and, with f, into
+  // f buffer fb
+  auto fetch = [&](int b, int64_t po, bool with_f, int fb) {
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      fx::cp_async8(lam_at(b, 1 + warp * R + r, 1 + lane), in + po + roff[r] + px);
+    if (warp == 0) {
+      fx::cp_async8(lam_at(b, 0, 1 + lane), in + po + rhalo);
+      fx::cp_async8(lam_at(b, 1 + lane, 0), in + po + chalo);
+    }
+    if (DOTS && with_f) {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        fx::cp_async8(sF + fb * SM::kFPlane + (warp * R + r) * 32 + lane,
+                      fstate + po + roff[r] + px);
+    }
+    fx::cp_async_commit();
+  };
+  // bring this thread's copies in lambda buffer b to the launch scale
+  auto rescale = [&](int b) {
+    auto sh = [&](int64_t* p) { *p = d > 0 ? (*p << d) : (*p >> (-d)); };
+#pragma unroll
+    for (int r = 0; r < R; ++r) sh(lam_at(b, 1 + warp * R + r, 1 + lane));
+    if (warp == 0) {
+      sh(lam_at(b, 0, 1 + lane));
+      sh(lam_at(b, 1 + lane, 0));
+    }
+  };
+
+  // The contraction terms are below 2^55 (|D| < 2^60, |F| < 2^59): int64
+  // sums take 32 planes of R = 4 rows before they go into the 128-bit ones.
   Acc128 acc[3];
+  int64_t part[3] = {0, 0, 0};
   unsigned long long my_or = 0ull;
-  for (int p = 0; p < nz_tile; ++p) {
+  // one plane: lambda buffers b (z) and bm (z-1), f buffer fb, output at po
+  auto compute = [&](auto full_tag, int b, int bm, int fb, int64_t po) {
+    constexpr bool kFull = decltype(full_tag)::value;
+    int64_t* dst = out + po + px;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      cur[r] = nx_cur[r];
-      fv[r] = nx_f[r];
-      xl[r] = nx_xl[r];
-    }
-    yh = nx_yh;
-    const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
-    if (p + 1 < nz_tile) load_plane(lz_next);
-    if (d != 0) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        cur[r] = d > 0 ? (cur[r] << d) : (cur[r] >> (-d));
-        xl[r] = d > 0 ? (xl[r] << d) : (xl[r] >> (-d));
-      }
-      yh = d > 0 ? (yh << d) : (yh >> (-d));
-    }
-    int64_t pz = 0, py = 0, pxx = 0;
-    int64_t* dst = out + plane_off(lz);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int64_t c = cur[r];
-      int64_t left = __shfl_up_sync(0xffffffffu, c, 1);
-      if (lane == 0) left = xl[r];
-      const int64_t upv = (r > 0) ? cur[r - 1] : yh;
-      const int64_t nv = fx::update(c, hist[r], upv, left, a);
-      if (row_mask & (1u << r)) {
+      const int row = 1 + warp * R + r;
+      const int64_t c = *lam_at(b, row, 1 + lane);
+      const int64_t Dz = *lam_at(bm, row, 1 + lane) - c;
+      const int64_t Dy = *lam_at(b, row - 1, 1 + lane) - c;
+      const int64_t Dx = *lam_at(b, row, lane) - c;
+      const int64_t nv = fixed_update_d(c, Dz, Dy, Dx, a.qz, a.qy, a.qx);
+      if (kFull || (row_mask & (1u << r))) {
         if (DOTS) {
           int32_t g1, g0;
-          split_balanced(fv[r], &g1, &g0);
-          pz += prod64(hist[r] - c, g1, g0);
-          py += prod64(upv - c, g1, g0);
-          pxx += prod64(left - c, g1, g0);
+          split_balanced(sF[fb * SM::kFPlane + (warp * R + r) * 32 + lane], &g1, &g0);
+          part[0] += prod64(Dz, g1, g0);
+          part[1] += prod64(Dy, g1, g0);
+          part[2] += prod64(Dx, g1, g0);
         }
         my_or |= (unsigned long long)(nv ^ (nv >> 63));
-        dst[roff[r] + px] = nv;
+        dst[roff[r]] = nv;
       }
-      hist[r] = c;
     }
-    acc[0].add(pz);
-    acc[1].add(py);
-    acc[2].add(pxx);
-    lz = lz_next;
+  };
+  // the tile lies inside the grid: every thread stores all R rows
+  const bool full = (tile_x + 1) * 32 <= a.nx && Y0 + SM::kRows <= a.ny;
+  const int64_t dz = a.fz ? -plane_sz : plane_sz;
+  const int64_t wrap_po = a.fz ? (int64_t)(a.nz - 1) * plane_sz : 0;
+
+  int lz = fx::wrap_mod(Z0 - 1, a.nz);
+  int64_t po = plane_off(lz);
+  int b = 0;  // lambda buffer of plane j (j mod 3)
+  fetch(0, po, false, 0);
+  for (int j = 0; j <= nz_tile; ++j) {
+    fx::cp_async_wait<0>();
+    if (d != 0) rescale(b);
+    __syncthreads();
+    const bool wraps = lz + 1 == a.nz;
+    lz = wraps ? 0 : lz + 1;
+    const int64_t po_next = wraps ? wrap_po : po + dz;
+    const int bn = b == 2 ? 0 : b + 1;
+    if (j < nz_tile) fetch(bn, po_next, true, (j + 1) & 1);
+    if (j > 0) {
+      const int bm = b == 0 ? 2 : b - 1;
+      if (full)
+        compute(std::true_type{}, b, bm, j & 1, po);
+      else
+        compute(std::false_type{}, b, bm, j & 1, po);
+      if (DOTS && (j & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          acc[k].add(part[k]);
+          part[k] = 0;
+        }
+      }
+    }
+    b = bn;
+    po = po_next;
+  }
+  if (DOTS) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[k].add(part[k]);
   }
 
-  // CTA sums of the three contractions, in units of 2^(64 - s - sf)
+  // CTA sums of the three contractions (exact integers in units of
+  // 2^(64 - s - sf)); one FP64 conversion per sum and CTA
   if (DOTS) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      double v = acc[j].to_double();
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) s_red[j][warp] = v;
+      acc[j].warp_sum();
+      if (lane == 0) {
+        s_red_lo[j][warp] = acc[j].lo;
+        s_red_hi[j][warp] = acc[j].hi;
+      }
     }
   }
   fx::cta_or<W>(my_or, s_or, &a.slot_out->m);  // contains __syncthreads
-  if (DOTS && tid == 0) {
-    const double unit = ldexp(1.0, 64 - s - sf);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      double t = 0.0;
-      for (int w = 0; w < W; ++w) t += s_red[j][w];
-      dpart[3 * blockIdx.x + j] += t * unit;
+  if (DOTS && tid < 3) {
+    Acc128 t;
+    for (int w = 0; w < W; ++w) {
+      Acc128 u;
+      u.lo = s_red_lo[tid][w];
+      u.hi = s_red_hi[tid][w];
+      t.add(u);
     }
+    dpart[3 * blockIdx.x + tid] += t.to_double() * pow2(64 - s - sf);
   }
 }
 
@@ -328,8 +402,29 @@ size_t adjoint_fixed_scratch_bytes(int seg_len) {
   return 6 * sizeof(ScaleSlot) + 4 * sizeof(int) + (size_t)(seg_len + 1) * sizeof(int);
 }
 
-// Tiling of the warp-independent one-step kernel: 32 columns x (kAR*kAW)
-// rows per CTA, tz planes chosen for about four waves of two CTAs per SM.
+// CTAs of the one-step kernel that fit on the current GPU at once.
+static int64_t step1_resident() {
+  static int per_sm = -1;  // benign race (idempotent)
+  if (per_sm < 0) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint_tile<kAR, kAW, true>,
+                                                      32 * kAW,
+                                                      AdjTileSmem<kAR, kAW, true>::bytes()) !=
+            cudaSuccess ||
+        occ < 1)
+      occ = 1;
+    per_sm = occ;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return (int64_t)per_sm * (sms > 0 ? sms : 1);
+}
+
+// Tiling of the one-step kernel: 32 columns x (kAR*kAW) rows per CTA and
+// as many z-slabs as fill one wave of resident CTAs (long z-runs amortise
+// each CTA's set-up, warm-up plane and final reduction; one wave has no
+// partial last wave), at least 4 planes each.
 // transpose = true: the adjoint (every upwind direction reversed).
 static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
   FixedArgs a = make_fixed_args(transpose ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
@@ -339,11 +434,10 @@ static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
   a.tiles_x = (a.nx + a.tx - 1) / a.tx;
   a.tiles_y = (a.ny + a.ty - 1) / a.ty;
   const int64_t txy = (int64_t)a.tiles_x * a.tiles_y;
-  const int64_t want = 4 * 2 * 152;
-  int64_t cz = (want + txy - 1) / txy;
+  int64_t cz = step1_resident() / txy;
+  if (cz > (a.nz + 3) / 4) cz = (a.nz + 3) / 4;
   if (cz < 1) cz = 1;
   int tz = (int)((a.nz + cz - 1) / cz);
-  if (tz < 4) tz = 4;
   if (tz > a.nz) tz = a.nz;
   a.tz = tz;
   a.tiles_z = (a.nz + tz - 1) / tz;
@@ -402,7 +496,8 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aF.slot_out = fr + ((k + 1) % 3);
       aF.slot_reset = fr + ((k + 2) % 3);
       aF.scale_log = logs + k;
-      k_adjoint_fixed<kAR, kAW, false><<<nblk, 32 * kAW, 0, st>>>(
+      k_adjoint_tile<kAR, kAW, false>
+          <<<nblk, 32 * kAW, AdjTileSmem<kAR, kAW, false>::bytes(), st>>>(
           io.states[k - 1], io.states[k], nullptr, nullptr, aF, nullptr);
       note_launch();
     }
@@ -416,9 +511,9 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aT.slot_in = lr + (li % 3);
       aT.slot_out = lr + ((li + 1) % 3);
       aT.slot_reset = lr + ((li + 2) % 3);
-      k_adjoint_fixed<kAR, kAW, true><<<nblk, 32 * kAW, 0, st>>>(io.lam[lc], io.lam[lc ^ 1],
-                                                               io.states[k], logs + k, aT,
-                                                               io.dpart);
+      k_adjoint_tile<kAR, kAW, true>
+          <<<nblk, 32 * kAW, AdjTileSmem<kAR, kAW, true>::bytes(), st>>>(
+              io.lam[lc], io.lam[lc ^ 1], io.states[k], logs + k, aT, io.dpart);
       note_launch();
       FDB_CUDA_TRY(cudaGetLastError());
       lc ^= 1;

@@ -18,12 +18,12 @@
 //
 // Update.  F' = F + sum_j a_j (F_up_j - F) with a_j in [0, 1] held in Q1.62
 // (A = a1 2^32 + a0, a0 balanced to [-2^31, 2^31)).  For D = d1 2^32 + d0:
-//   A D / 2^64 = a1 d1 + (a0 d1 + a1 d0 2^-32) 2^-32 + ...
-// the a1 d1 products accumulate exactly with IMAD.WIDE; the a0 d1 and a1 d0
-// partial products of the three axes are summed exactly in two 64-bit
-// accumulators seeded with 2^31 and their high words taken (round to
-// nearest); F' = F + 4 * sum.  The rounding is unbiased and a zero
-// difference contributes exactly zero.
+//   A D / 2^64 = a1 d1 + (a1 d0 + a0 d1) 2^-32 + a0 d0 2^-64
+// the a1 d1 products are summed exactly; the six a1 d0 and a0 d1 partial
+// products of the three axes are summed exactly in one offset unsigned
+// 64-bit word whose high word is taken (one rounding to nearest);
+// F' = F + 4 * sum (fixed_point.cuh fixed_update).  The rounding is unbiased
+// and a zero difference contributes exactly zero.
 //
 // Geometry.  Axes are relabelled so that every upstream neighbour is at -1
 // (axis j reversed when v_j < 0, upwind.cxx:34-35).  A CTA of W warps owns an

@@ -53,38 +53,11 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ int64_t mad_s(int32_t a, int32_t b, int64_t c) {
-  int64_t d;
-  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ uint64_t mad_u(uint32_t a, uint32_t b, uint64_t c) {
-  uint64_t d;
-  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-  return d;
-}
-
-// One level for one cell: F' = F + 4 * sum_j A_j D_j / 2^64 with D_j =
-// F_up_j - F.  The a1*d1 products accumulate exactly; the two families of
-// 32x32 partial products (a0*d1 signed, a1*d0 unsigned) are each summed
-// exactly in 64 bits from 2^31 and their high words taken, i.e. rounded to
-// nearest: unbiased, and exactly zero when every D_j is zero.
+// One level for one cell (fixed_point.cuh fixed_update: nine 32x32->64-bit
+// products, one rounding, exactly F when every difference is zero).
 __device__ __forceinline__ int64_t update(int64_t c, int64_t zb, int64_t up, int64_t left,
                                           const FixedArgs& a) {
-  const int64_t Dz = zb - c, Dy = up - c, Dx = left - c;
-  const int32_t z1 = (int32_t)(Dz >> 32), y1 = (int32_t)(Dy >> 32), x1 = (int32_t)(Dx >> 32);
-  const uint32_t z0 = (uint32_t)Dz, y0 = (uint32_t)Dy, x0 = (uint32_t)Dx;
-  int64_t acc = mad_s(a.qz.a1, z1, 0);
-  acc = mad_s(a.qy.a1, y1, acc);
-  acc = mad_s(a.qx.a1, x1, acc);
-  int64_t h = mad_s(a.qz.a0, z1, 0x80000000ll);
-  h = mad_s(a.qy.a0, y1, h);
-  h = mad_s(a.qx.a0, x1, h);
-  uint64_t v = mad_u((uint32_t)a.qz.a1, z0, 0x80000000ull);
-  v = mad_u((uint32_t)a.qy.a1, y0, v);
-  v = mad_u((uint32_t)a.qx.a1, x0, v);
-  acc += (h >> 32) + (int64_t)(v >> 32);
-  return c + acc * 4;
+  return fixed_update(c, zb, up, left, a.qz, a.qy, a.qx);
 }
 
 // Dynamic shared memory of one CTA: plane prefetch [2][R][threads] (cp.async

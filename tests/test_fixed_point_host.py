@@ -24,14 +24,10 @@ double t_to_double(int64_t F, int s) { return fdb::to_double(F, s); }
 void t_qcoeff(double a, int32_t* a1, int32_t* a0) {
   fdb::QCoeff q = fdb::make_qcoeff(a); *a1 = q.a1; *a0 = q.a0;
 }
-// host restatement of mul_q with the same 32-bit pieces
-int64_t t_mul_q(int64_t D, int32_t a1, int32_t a0) {
-  const int32_t d1 = (int32_t)(D >> 32);
-  const uint32_t d0 = (uint32_t)D;
-  const int64_t w = (int64_t)a1 * (int64_t)d1;
-  const int32_t h = (int32_t)(((int64_t)a0 * (int64_t)d1) >> 32);
-  const uint32_t u = (uint32_t)(((uint64_t)(uint32_t)a1 * (uint64_t)d0) >> 32);
-  return w + (int64_t)h + (int64_t)(uint64_t)u;
+// the kernels' cell update (the same source, compiled for the host)
+int64_t t_update(int64_t c, int64_t zb, int64_t up, int64_t left, const double* a) {
+  return fdb::fixed_update(c, zb, up, left, fdb::make_qcoeff(a[0]), fdb::make_qcoeff(a[1]),
+                           fdb::make_qcoeff(a[2]));
 }
 }
 """
@@ -53,8 +49,8 @@ def fx():
     lib.t_to_double.restype = ctypes.c_double
     lib.t_qcoeff.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_int32),
                              ctypes.POINTER(ctypes.c_int32)]
-    lib.t_mul_q.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32]
-    lib.t_mul_q.restype = ctypes.c_int64
+    lib.t_update.argtypes = [ctypes.c_int64] * 4 + [ctypes.POINTER(ctypes.c_double)]
+    lib.t_update.restype = ctypes.c_int64
     return lib
 
 
@@ -92,18 +88,37 @@ def test_round_trip_exact_for_53_bit_values(fx):
         assert fx.t_to_double(F, 60) == float(f)
 
 
-@pytest.mark.parametrize("a", [0.0, 0.5, 0.35, 0.15, 1.0, 1.5, 0.8 * 0.5, 1e-7, 0.999999999])
-def test_mul_q_error_bound(fx, a):
+@pytest.mark.parametrize("a", [0.0, 0.5, 0.35, 0.15, 1.0, 0.8 * 0.5, 1e-7, 0.999999999])
+def test_qcoeff_halves(fx, a):
     a1 = ctypes.c_int32()
     a0 = ctypes.c_int32()
     fx.t_qcoeff(a, ctypes.byref(a1), ctypes.byref(a0))
     A = (a1.value << 32) + a0.value
     assert abs(Fraction(A) - Fraction(a) * 2 ** 62) < 1
-    rng = np.random.default_rng(4)
-    Ds = [int(x) for x in rng.integers(-(1 << 61), 1 << 61, size=300)] + [0, 1, -1]
-    for D in Ds:
-        got = fx.t_mul_q(D, a1.value, a0.value)
-        exact = Fraction(A * D, 1 << 64)
-        assert -Fraction(5, 2) <= Fraction(got) - exact <= Fraction(1, 2), (a, D)
-        if D == 0:
-            assert got == 0
+    assert 0 <= a1.value <= 1 << 30 and -(1 << 31) <= a0.value < 1 << 31
+
+
+@pytest.mark.parametrize("a", [(0.5, 0.35, 0.15), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0),
+                               (1e-7, 0.999999999, 0.4), (0.3, 0.0, 1.0)])
+def test_update_error_bound(fx, a):
+    """F' within 8 units of F + sum_j a_j D_j (the Q1.62 coefficients), also at
+    the range limits |F| < 2^59, and exactly F when every difference is 0."""
+    q = []
+    for aj in a:
+        a1 = ctypes.c_int32()
+        a0 = ctypes.c_int32()
+        fx.t_qcoeff(aj, ctypes.byref(a1), ctypes.byref(a0))
+        q.append((a1.value << 32) + a0.value)
+    av = (ctypes.c_double * 3)(*a)
+    lim = (1 << 59) - 1
+    rng = np.random.default_rng(5)
+    cases = [tuple(int(x) for x in rng.integers(-lim, lim, size=4, endpoint=True))
+             for _ in range(400)]
+    cases += [(lim, -lim, -lim, -lim), (-lim, lim, lim, lim), (0, lim, -lim, lim),
+              (lim, lim, lim, lim), (-lim, -lim, -lim, -lim), (12345, 12345, 12345, 12345)]
+    for c, zb, up, left in cases:
+        got = fx.t_update(c, zb, up, left, av)
+        exact = c + Fraction(4 * sum(A * (u - c) for A, u in zip(q, (zb, up, left))), 1 << 64)
+        assert abs(Fraction(got) - exact) <= 8, (a, c, zb, up, left)
+        if zb == up == left == c:
+            assert got == c
