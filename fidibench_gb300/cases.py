@@ -5,6 +5,9 @@ on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
                 adjoint calls of S steps with one checkpoint segment
   advect N S  : N^3 sphere + noise field, v = (1, -0.7, 0.3), dt = 0.5/N,
                 three advect calls of S steps
+  batch C S   : C seeded instances with axes in [32, 160] (the benchmark's
+                generator), three batched advects of S steps (depth 4,
+                shape 4x8 with shared-memory history)
 """
 from __future__ import annotations
 
@@ -39,15 +42,27 @@ def advect_case(n: int, steps: int) -> float:
     return cs
 
 
+def batch_case(count: int, steps: int) -> float:
+    from fidibench_gb300.batch import Batch, random_instances
+    specs = random_instances(count, 20261203)
+    b = Batch([(s["v"], s["L"], s["n"]) for s in specs])
+    for k, s in enumerate(specs):
+        b.init_sphere(k, s["center"], s["radius"], 0.0, 20261203 + k)
+    b.set_tuning(depth=4, shape=4, tile_z=0)
+    dts = [s["dt"] for s in specs]
+    for _ in range(3):
+        b.advect(steps, dts)
+    cs = float(sum(b.checksums()))
+    b.close()
+    return cs
+
+
 def main(argv: list[str]) -> int:
-    if len(argv) != 3 or argv[0] not in ("adjoint", "advect"):
+    cases = {"adjoint": adjoint_case, "advect": advect_case, "batch": batch_case}
+    if len(argv) != 3 or argv[0] not in cases:
         print(__doc__)
         return 2
-    n, steps = int(argv[1]), int(argv[2])
-    if argv[0] == "adjoint":
-        print(adjoint_case(n, steps))
-    else:
-        print(advect_case(n, steps))
+    print(cases[argv[0]](int(argv[1]), int(argv[2])))
     return 0
 
 

@@ -61,8 +61,10 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
+// 4-row shapes: at least 32 warps per SM (64 registers per thread, no
+// spills); 8-row shapes: 16 warps (their rows need the registers)
 template <int K, int R, int W>
-__global__ void __launch_bounds__(32 * W, 1)
+__global__ void __launch_bounds__(32 * W, (R > 4 ? 512 : 1024) / (32 * W))
 k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_inst,
               int items_per_block, int nblocks, int steps, int64_t* arena0, int64_t* arena1,
               ScaleSlot* slots, unsigned* done, unsigned* queue, int* err, unsigned wait_bias,
