@@ -86,13 +86,14 @@ class Upwind:
 
     def set_tile_z(self, tile_z: int) -> None:
         """Most output planes one CTA of the fixed-point kernel takes along
-        the slowest axis (0 = automatic: an equal share per resident CTA)."""
+        the slowest axis (0 = automatic: z-slabs that shrink towards the end
+        of the grid)."""
         check(lib.fdb_upwind_set_tuning(self._h, 1, int(tile_z)))
 
     def set_shape(self, shape: int) -> None:
         """Fixed-point kernel CTA shape: 0 = 8 rows x 8 warps, 1 = 4 x 16 (plane
-        history in registers), 2 = 8 x 8, 3 = 4 x 16 (history in shared
-        memory), -1 = automatic."""
+        history in registers), 2 = 8 x 8, 3 = 4 x 16, 4 = 4 x 8 (history in
+        shared memory), -1 = automatic (3)."""
         check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
 
     def set_velocity(self, velocity) -> None:

@@ -107,9 +107,10 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
 
 /* Launch-shape tuning of the FIXED kernel (the autotuner's knobs).
  *  FDB_TUNE_TILE_Z : single field: most output planes one CTA takes along
- *                    the slowest axis (0 = auto: every resident CTA takes an
- *                    equal share in one wave); batches: output planes per
- *                    work item (0 = auto).
+ *                    the slowest axis (0 = auto: a quarter of the planes per
+ *                    resident CTA, at least 32; the last z-slabs shrink so
+ *                    that the last wave is short); batches: output planes
+ *                    per work item (0 = auto).
  *  FDB_TUNE_SHAPE  : rows per thread x warps per CTA and where the plane
  *                    history lives: 0 = 8x8 registers, 1 = 4x16 registers,
  *                    2 = 8x8 shared memory, 3 = 4x16 shared memory,
