@@ -233,3 +233,40 @@ class Upwind:
         check(lib.fdb_upwind_adjoint_timings(self._h, ms.ctypes.data))
         return {"forward_ms": float(ms[0]), "recompute_ms": float(ms[1]),
                 "adjoint_ms": float(ms[2])}
+
+
+def main(argv=None) -> int:
+    """Command line of the reference's Python driver (upwind/python/upwind.py:
+    88-126): ``N [numTimeSteps=100] [vtk]`` on the periodic unit cube with
+    N^3 cells, velocity (1, 1, 1) and courant 0.1, one advect(dt) call per
+    step, then ``check sum:`` (and up.vtk with ``vtk``)."""
+    import sys
+    args = sys.argv[1:] if argv is None else list(argv)
+    if len(args) < 1:
+        print("must specify number of cells in each direction.")
+        return 1
+    ndims = 3
+    numCells = [int(args[0])] * ndims
+    print("number of cells: ", numCells)
+    numTimeSteps = int(args[1]) if len(args) > 1 else 100
+    print("number of time steps: ", numTimeSteps)
+    doVtk = len(args) > 2 and args[2] == "vtk"
+    velocity = np.ones((ndims,), np.float64)
+    lengths = np.ones((ndims,), np.float64)
+    courant = 0.1
+    dt = float("inf")
+    for j in range(ndims):
+        dx = lengths[j] / float(numCells[j])
+        dt = min(courant * dx / velocity[j], dt)
+    up = Upwind(velocity, lengths, numCells)
+    for _ in range(numTimeSteps):
+        up.advect(dt)
+    print("check sum: ", up.checksum())
+    if doVtk:
+        up.saveVTK("up.vtk")
+    up.close()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

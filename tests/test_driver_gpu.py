@@ -79,3 +79,25 @@ def test_python_mirror_vtk_matches(tmp_path, fdb):
     assert ours.splitlines()[2:] == ref.splitlines()[2:]
     up.close()
     assert np.isfinite(up.ntot)
+
+
+def test_python_cli_matches_reference_contract(tmp_path):
+    """`python -m fidibench_gb300.upwind N S [vtk]`: the reference Python
+    driver's command line and output lines (upwind/python/upwind.py:88-126;
+    ctest upwindPython regex `[Cc]heck sum:[ ]*[1\\.0|0\\.999]`)."""
+    import sys
+    r = subprocess.run([sys.executable, "-m", "fidibench_gb300.upwind", "32", "10", "vtk"],
+                       cwd=tmp_path, env={**os.environ, "PYTHONPATH": ROOT},
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == "number of cells:  [32, 32, 32]"
+    assert lines[1] == "number of time steps:  10"
+    assert re.search(r"[Cc]heck sum:[ ]*[1\.0|0\.999]", lines[2])
+    assert abs(float(lines[2].split()[-1]) - 1.0) < 1e-12
+    assert (tmp_path / "up.vtk").exists()
+    r = subprocess.run([sys.executable, "-m", "fidibench_gb300.upwind"], cwd=tmp_path,
+                       env={**os.environ, "PYTHONPATH": ROOT}, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 1
+    assert "must specify number of cells" in r.stdout
