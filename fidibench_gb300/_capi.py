@@ -1,4 +1,5 @@
-"""ctypes binding of libfdb_upwind.so (the C-ABI in include/fdb_upwind.h).
+"""ctypes binding of libfdb_upwind.so (the C-ABI in include/fdb_upwind.h and
+include/fdb_filter.h).
 
 The library is loaded from the package's in-tree ``_lib/`` directory.  There
 is no fallback: if the shared library is missing or was built for another
@@ -71,6 +72,19 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_adjoint": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _vp, _int, _int]),
     "fdb_upwind_adjoint_step": (_int, [_vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
     "fdb_upwind_adjoint_timings": (_int, [_vp, _vp]),
+    # include/fdb_filter.h
+    "fdb_filter_create": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, ctypes.POINTER(_vp)]),
+    "fdb_filter_destroy": (_int, [_vp]),
+    "fdb_filter_set_in_data": (_int, [_vp, _vp, _int]),
+    "fdb_filter_get_data": (_int, [_vp, _int, _vp, _int]),
+    "fdb_filter_apply": (_int, [_vp]),
+    "fdb_filter_copy_out_to_in": (_int, [_vp]),
+    "fdb_filter_iterate": (_int, [_vp, _int]),
+    "fdb_filter_checksum": (_int, [_vp, _int, _dp]),
+    "fdb_filter_set_wrap": (_int, [_vp, _int]),
+    "fdb_filter_set_stream": (_int, [_vp, _vp]),
+    "fdb_filter_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
+    "fdb_filter_synchronize": (_int, [_vp]),
 }
 
 

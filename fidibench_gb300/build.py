@@ -25,6 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_lib", "obj")
 LIB = os.path.join(PKG, "_lib", "libfdb_upwind.so")
 DRIVER = os.path.join(PKG, "_lib", "upwindCxx")
+DRIVERS = ("upwindCxx", "laplacian")  # fidibench_gb300/drivers/<name>.cpp -> _lib/<name>
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -76,11 +77,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
 
-    drv_src = os.path.join(PKG, "drivers", "upwindCxx.cpp")
-    if os.path.exists(drv_src):
-        deps = [drv_src, LIB] + glob.glob(os.path.join(INCLUDE, "fidibench_gb", "*.h"))
-        if force or not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < _newest(deps):
-            _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, drv_src, "-o", DRIVER,
+    for name in DRIVERS:
+        drv_src = os.path.join(PKG, "drivers", name + ".cpp")
+        exe = os.path.join(PKG, "_lib", name)
+        deps = [drv_src, LIB] + glob.glob(os.path.join(INCLUDE, "fidibench_gb", "*.h")) + \
+            glob.glob(os.path.join(INCLUDE, "*.h")) + \
+            glob.glob(os.path.join(PKG, "drivers", "*.h"))
+        if force or not os.path.exists(exe) or os.path.getmtime(exe) < _newest(deps):
+            _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, drv_src, "-o", exe,
                   "-L" + os.path.dirname(LIB), "-lfdb_upwind", "-Wl,-rpath,$ORIGIN"])
     return LIB
 

@@ -9,7 +9,6 @@
 // positional "32 10" of the ctest cases) are ignored; an unknown -option prints
 // "<arg> is not a valid option." and the help text.  Added options:
 //   -arith <auto|exact|fma|fixed>  -courant <double> (0.1)  -json
-#include <cctype>
 #include <chrono>
 #include <cstdlib>
 #include <iostream>
@@ -19,44 +18,12 @@
 #include <vector>
 
 #include "fidibench_gb/Upwind.h"
+#include "options.h"
 
 namespace {
 
-struct Options {
-  std::map<std::string, std::string> values;  // valued options
-  std::map<std::string, bool> flags;          // toggles
-  std::map<std::string, std::string> help;
-};
-
-bool is_option_name(const std::string& a) {
-  return a.size() >= 2 && a[0] == '-' && !std::isdigit((unsigned char)a[1]);
-}
-
-bool parse(Options& o, int argc, char** argv) {
-  for (int a = 1; a < argc; ++a) {
-    std::string arg(argv[a]);
-    if (is_option_name(arg) && !o.values.count(arg) && !o.flags.count(arg)) {
-      std::cout << arg << " is not a valid option.\n";
-      return false;
-    }
-  }
-  for (int a = 1; a < argc; ++a) {
-    std::string arg(argv[a]);
-    if (o.values.count(arg) && a + 1 < argc) o.values[arg] = argv[a + 1];
-    if (o.flags.count(arg)) o.flags[arg] = !o.flags[arg];
-  }
-  return true;
-}
-
-void print_help(const Options& o, const char* exe) {
-  std::cout << "Purpose: benchmark finite difference operations (GB300 library).\n";
-  std::cout << exe << " [options]\nUsage:\n";
-  for (const auto& kv : o.values)
-    std::cout << "\t" << kv.first << " <value> " << o.help.at(kv.first) << " (" << kv.second
-              << ")\n";
-  for (const auto& kv : o.flags)
-    std::cout << "\t" << kv.first << ' ' << o.help.at(kv.first) << " (" << kv.second << ")\n";
-}
+using fdb_drivers::Options;
+using fdb_drivers::parse;
 
 int arith_code(const std::string& s) {
   if (s == "exact") return FDB_ARITH_EXACT;
@@ -90,7 +57,8 @@ int main(int argc, char** argv) {
   const bool success = parse(o, argc, argv);
   if (!success || o.flags["-h"]) {
     if (!success) std::cerr << "ERROR when parsing command line arguments\n";
-    print_help(o, argv[0]);
+    fdb_drivers::print_help(o, "Purpose: benchmark finite difference operations (GB300 library).",
+                            argv[0]);
     return 0;
   }
   const int numTimeSteps = std::atoi(o.values["-numSteps"].c_str());

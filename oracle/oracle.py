@@ -126,6 +126,66 @@ class Port:
     def max_threads(self) -> int:
         return self.lib.fdbo_max_threads()
 
+    # -- stencil Filter (filter_oracle.c) ----------------------------------------------
+    def _filter_lib(self):
+        lib = self.lib
+        if not getattr(self, "_filter_ready", False):
+            _ip = ctypes.POINTER(ctypes.c_int)
+            lib.fdbo_filter_apply.argtypes = [ctypes.c_int, _u64p, ctypes.c_int, _ip, _dp, _dp,
+                                              _dp, ctypes.c_int]
+            lib.fdbo_filter_apply.restype = ctypes.c_int
+            lib.fdbo_filter_checksum.argtypes = [_dp, ctypes.c_uint64]
+            lib.fdbo_filter_checksum.restype = ctypes.c_double
+            lib.fdbo_filter_sin_input.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp]
+            lib.fdbo_filter_sin_input.restype = ctypes.c_int
+            lib.fdbo_stencil_order.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _ip, _ip]
+            lib.fdbo_stencil_order.restype = ctypes.c_int
+            self._filter_ready = True
+        return lib
+
+    def filter_apply(self, dims, stencil, f_in, periodic: bool = False) -> np.ndarray:
+        """One applyFilter of `stencil` ({offset tuple: weight} or a list of
+        (offset, weight) pairs, insertion order kept) on the column-major
+        field f_in; periodic=False reproduces the reference's index wrap."""
+        lib = self._filter_lib()
+        items = list(stencil.items()) if hasattr(stencil, "items") else list(stencil)
+        dims = _u64(dims)
+        offs = np.ascontiguousarray(np.array([o for o, _ in items], dtype=np.int32).reshape(-1))
+        w = _f64([x for _, x in items])
+        fi = _f64(f_in).reshape(-1)
+        out = np.empty_like(fi)
+        rc = lib.fdbo_filter_apply(len(dims), dims.ctypes.data_as(_u64p), len(items),
+                                   offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(w),
+                                   _ptr(fi), _ptr(out), 1 if periodic else 0)
+        if rc:
+            raise ValueError("oracle filter rejected its arguments")
+        return out
+
+    def filter_checksum(self, f) -> float:
+        f = _f64(f).reshape(-1)
+        return self._filter_lib().fdbo_filter_checksum(_ptr(f), f.size)
+
+    def filter_sin_input(self, dims, xmins, xmaxs) -> np.ndarray:
+        lib = self._filter_lib()
+        dims, lo, hi = _u64(dims), _f64(xmins), _f64(xmaxs)
+        f = np.empty(int(np.prod(dims)), dtype=np.float64)
+        lib.fdbo_filter_sin_input(len(dims), dims.ctypes.data_as(_u64p), _ptr(lo), _ptr(hi),
+                                  _ptr(f))
+        return f
+
+    def stencil_order(self, offsets) -> list[int]:
+        """Term indices in the reference's std::map order (first insertion of
+        a repeated offset wins)."""
+        lib = self._filter_lib()
+        o = np.ascontiguousarray(np.array(offsets, dtype=np.int32))
+        nd = o.shape[1]
+        order = np.zeros(len(o), dtype=np.int32)
+        nu = ctypes.c_int()
+        ip = ctypes.POINTER(ctypes.c_int)
+        lib.fdbo_stencil_order(nd, len(o), o.ctypes.data_as(ip), order.ctypes.data_as(ip),
+                               ctypes.byref(nu))
+        return [int(x) for x in order[:nu.value]]
+
 
 class Reference:
     """The reference's own Upwind<NDIMS> (ref_harness.cpp), when built here."""
