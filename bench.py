@@ -361,6 +361,84 @@ def bench_adjoint(stream) -> dict:
             "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "grad_v": [float(x) for x in gv]}
 
 
+LAP_N = 8000   # the reference laplacian driver's defaults (laplacian/cxx/laplacian.cxx:41-43)
+LAP_DIMS = 2
+LAP_ITERS = 10
+
+
+def bench_laplacian(stream, cpu: bool) -> dict:
+    """Stencil Filter: the reference laplacian driver's default case, 2-D
+    8000^2 on the unit square, input prod_i sin(2 pi x_i) at the cell centres,
+    stencil -4 at the centre and +1 at +-1 along each axis, the reference's
+    index wrap, timed loop 10 x (applyFilter; copyOutToIn).  Also the apply
+    kernel alone (iterate: the copy becomes a buffer swap) against the FP64
+    pipe (2 operations/clk/SM) and HBM; with the CPU leg, one apply checked
+    bit for bit against the CPU restatement and that restatement's own rate."""
+    import torch
+    from fidibench_gb300.filter import Filter, laplacian_stencil
+
+    dims = (LAP_N,) * LAP_DIMS
+    st = laplacian_stencil(LAP_DIMS)
+    x = (np.arange(LAP_N, dtype=np.float64) + 0.5) * (1.0 / LAP_N)
+    s = np.sin(2.0 * np.pi * x)
+    f0 = np.ascontiguousarray((s[:, None] * s[None, :]).reshape(-1))
+    cells = float(f0.size)
+    flt = Filter(dims, [0.0] * LAP_DIMS, [1.0] * LAP_DIMS, st)
+    flt.set_stream(stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        flt.set_in_data(f0)
+        fn()  # warm-up
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def loop():
+        for _ in range(LAP_ITERS):
+            flt.applyFilter()
+            flt.copyOutToIn()
+
+    ms_loop = timed(loop, 3) / LAP_ITERS
+    ms_apply = timed(lambda: flt.iterate(LAP_ITERS), 3) / LAP_ITERS
+    fp64_per_cell = sum(1 for w in st.values() if w not in (1.0, -1.0)) + (len(st) - 1)
+    clock_hz = 2.07e9
+    fp64_peak = 2.0 * 152 * clock_hz / 1e9  # GFLOP/s
+    out = {
+        "workload": f"laplacian{LAP_DIMS}d_{LAP_N}^{LAP_DIMS}_{LAP_ITERS}iters",
+        "cells": int(cells), "iterations": LAP_ITERS, "wrap": "reference",
+        "gcups_apply_copy_loop": cells / (ms_loop * 1e-3) / 1e9,
+        "gcups_apply": cells / (ms_apply * 1e-3) / 1e9,
+        "ms_per_apply": ms_apply,
+        "fp64_ops_per_cell": fp64_per_cell,
+        "fp64_gflops": fp64_per_cell * cells / (ms_apply * 1e-3) / 1e9,
+        "fp64_frac_of_pipe": fp64_per_cell * cells / (ms_apply * 1e-3) / 1e9 / fp64_peak,
+        "hbm_gbs_apply": 16.0 * cells / (ms_apply * 1e-3) / 1e9,
+        "bound": "fp64 pipe (bit-identical products and sums in the reference's order)",
+    }
+    if cpu:
+        from oracle import Port
+        port = Port()
+        flt.set_in_data(f0)
+        flt.applyFilter()
+        got = flt.out_data
+        t0 = time.perf_counter()
+        ref = port.filter_apply(dims, st, f0)
+        t_cpu = time.perf_counter() - t0
+        out["bit_identical_vs_cpu"] = bool(np.array_equal(got, ref))
+        out["cpu_baseline"] = {"value": cells / t_cpu / 1e9, "unit": "GCUPS",
+                               "cores": port.max_threads(), "kind": "port",
+                               "sample": "one applyFilter at 8000^2 (oracle/filter_oracle.c, "
+                                         "OpenMP, -O3 -ffp-contract=off)"}
+    flt.close()
+    return out
+
+
 def run_reference_arm(args, ws, rank) -> None:
     if rank != 0:
         return
@@ -400,6 +478,8 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-recovery", action="store_true",
                     help="skip the batched adjoint (gradient-descent recovery) leg")
+    ap.add_argument("--no-laplacian", action="store_true",
+                    help="skip the stencil Filter (laplacian driver) leg")
     ap.add_argument("--n", type=int, default=512, help="cube size (profiling only)")
     ap.add_argument("--tz", type=int, default=0, help="fixed kernel z-tile override")
     ap.add_argument("--shape", type=int, default=-1, help="fixed kernel CTA shape (0..2)")
@@ -513,6 +593,9 @@ def main() -> None:
         # 100 steps, 20 gradient-descent iterations through the autograd Function
         from fidibench_gb300.recovery import recover
         recovery = recover(count=64, n=128, steps=100, iters=20, seed=SEED)
+    laplacian = None
+    if not args.no_laplacian and rank == 0:
+        laplacian = bench_laplacian(stream, cpu=not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -543,6 +626,7 @@ def main() -> None:
             "batched": batched,
             "adjoint": adjoint,
             "batched_adjoint_recovery": recovery,
+            "stencil_filter": laplacian,
         }
         print(json.dumps(line))
     if dist is not None:
