@@ -129,22 +129,22 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   const int px = a.fx ? a.nx - 1 - lx : lx;
   const bool out_x = (lane >= K) && (X0 + lane - K < a.nx);
 
-  // offset (py * nx + px) of row r; rows that do not wrap form an arithmetic
-  // progression, so only the first offset and the step stay in registers
+  // offset (py * nx + px) of each of this thread's rows, wrapped once here:
+  // the rows stay the same for the whole z-march
   const int ly0 = Y0 - K + warp * R;
-  const bool rows_linear = (ly0 >= 0) && (ly0 + R - 1 < a.ny);
-  const int rstep = a.fy ? -a.nx : a.nx;
-  const int roff0 = (a.fy ? a.ny - 1 - wrap_mod(ly0, a.ny) : wrap_mod(ly0, a.ny)) * a.nx + px;
-  auto row_off = [&](int r) -> int {
-    if (rows_linear) return roff0 + r * rstep;
-    const int ly = wrap_mod(ly0 + r, a.ny);
-    return (a.fy ? a.ny - 1 - ly : ly) * a.nx + px;
-  };
+  int roff[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    int ly = ly0 + r;
+    ly = ly < 0 ? ly + a.ny : (ly >= a.ny ? ly - a.ny : ly);  // |ly0| < ny: one wrap at most
+    if (ly < 0 || ly >= a.ny) ly = wrap_mod(ly, a.ny);         // grids shorter than the tile
+    roff[r] = (a.fy ? a.ny - 1 - ly : ly) * a.nx + px;
+  }
+  // physical offset of the plane at logical z, advanced plane by plane
   const int64_t plane_sz = (int64_t)a.ny * a.nx;
+  const int64_t dz = a.fz ? -plane_sz : plane_sz;
+  const int64_t po_wrap = a.fz ? (int64_t)(a.nz - 1) * plane_sz : 0;  // logical z = 0
   const int nplanes = nout + K;
-  auto plane_ptr = [&](const int64_t* base, int lz) {
-    return base + (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
-  };
   // rows this thread writes: bit r set when row r lies in the tile and the grid
   unsigned row_mask = 0u;
 #pragma unroll
@@ -169,26 +169,29 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
 
   // logical z of the plane being computed; advanced by one per iteration
   int lz = wrap_mod(Z0 - K, a.nz);
+  int64_t po = (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
   {
-    const int64_t* src = plane_ptr(in, lz);
+    const int64_t* src = in + po;
     if (LOADER == kLoadCpAsync) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], src + row_off(r));
+      for (int r = 0; r < R; ++r) cp_async8(&s_pre[0][r][tid], src + roff[r]);
       cp_async_commit();
     } else {
 #pragma unroll
-      for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + row_off(r));
+      for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + roff[r]);
     }
   }
 
   int parity = 0;
   for (int p = 0; p < nplanes; ++p) {
-    const int lz_next = (lz + 1 == a.nz) ? 0 : lz + 1;
+    const bool wraps = lz + 1 == a.nz;
+    const int lz_next = wraps ? 0 : lz + 1;
+    const int64_t po_next = wraps ? po_wrap : po + dz;
     if (LOADER == kLoadCpAsync) {
       if (p + 1 < nplanes) {
-        const int64_t* src = plane_ptr(in, lz_next);
+        const int64_t* src = in + po_next;
 #pragma unroll
-        for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], src + row_off(r));
+        for (int r = 0; r < R; ++r) cp_async8(&s_pre[(p + 1) & 1][r][tid], src + roff[r]);
       }
       cp_async_commit();
       cp_async_wait<1>();
@@ -198,9 +201,9 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
 #pragma unroll
       for (int r = 0; r < R; ++r) cur[r] = pre[r];
       if (p + 1 < nplanes) {
-        const int64_t* src = plane_ptr(in, lz_next);
+        const int64_t* src = in + po_next;
 #pragma unroll
-        for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + row_off(r));
+        for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + roff[r]);
       }
     }
     if (in_f64) {
@@ -249,20 +252,21 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
       }
     }
     if (p >= K) {
-      int64_t* dst = const_cast<int64_t*>(plane_ptr(out, lz));
+      int64_t* dst = out + po;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (row_mask & (1u << r)) {
           const int64_t v = cur[r];
           my_or |= (unsigned long long)(v ^ (v >> 63));
           if (out_f64)
-            dst[row_off(r)] = __double_as_longlong(to_double(v, s));
+            dst[roff[r]] = __double_as_longlong(to_double(v, s));
           else
-            dst[row_off(r)] = v;
+            dst[roff[r]] = v;
         }
       }
     }
     lz = lz_next;
+    po = po_next;
   }
   if (LOADER == kLoadCpAsync) cp_async_wait<0>();
 }
