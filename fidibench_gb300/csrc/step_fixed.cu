@@ -206,13 +206,37 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
 
 namespace {
 
-int default_depth() { return kMaxDepth; }
+// Default shape: 4 rows x 8 warps with the plane history in shared memory (32
+// x 32 computed cells per tile; the fastest measured shape at 160^3 - 512^3).
+constexpr int kDefaultShape = fx::kR4W8S;
+
+// Steps per launch for the default shape: the K that minimises the computed
+// tiles times the per-launch cost,
+//   ceil(nx / (32 - K)) * ceil(ny / (32 - K)) * (1 + 0.5 / K),
+// where 0.5 is the per-plane work (load, scale, store) in units of one
+// level's update (fitted to 160^3 .. 512^3 sweeps of K = 2..4, whose
+// winners this picks: 4 at 160, 3 at 256, 2 at 384, 3 at 512); ties go to
+// the deeper K.
+int default_depth(const Geom& g) {
+  int best = kMaxDepth;
+  double best_cost = 0.0;
+  for (int K = kMaxDepth; K >= 2; --K) {
+    const double w = 32.0 - K;
+    const double tiles = std::ceil(g.nx / w) * std::ceil(g.ny / w);
+    const double cost = tiles * (1.0 + 0.5 / K);
+    if (K == kMaxDepth || cost < best_cost) {
+      best = K;
+      best_cost = cost;
+    }
+  }
+  return best;
+}
 
 }  // namespace
 
 int fixed_supported(const Geom& g, const Coeffs3& c, int depth) {
   if (g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "fixed kernel serves ndims <= 3");
-  const int K = depth > 0 ? depth : default_depth();
+  const int K = depth > 0 ? depth : default_depth(g);
   if (K > kMaxDepth) return fail(FDB_ERR_UNSUPPORTED, "fixed kernel temporal depth must be <= 4");
   const double as[3] = {c.az, c.ay, c.ax};
   for (double x : as)
@@ -251,10 +275,8 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   if (steps <= 0) return FDB_OK;
   ScaleSlot* slots = (ScaleSlot*)d_scratch;
   int* err = fixed_error_word(d_scratch);
-  const int K = tune.depth > 0 ? tune.depth : default_depth();
-  // default: 4 rows x 16 warps with the plane history in shared memory (the
-  // fastest measured shape at 512^3, K = 4)
-  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : fx::kR4W16S;
+  const int K = tune.depth > 0 ? tune.depth : default_depth(g);
+  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : kDefaultShape;
   int i0 = (scale_slot && *scale_slot >= 0) ? *scale_slot : -1;
   if (i0 < 0) {
     k_slots_init<<<1, 32, 0, s>>>(slots);

@@ -231,25 +231,28 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
 #pragma unroll
         for (int r = 0; r < R; ++r) zb[r] = s_hist[t][r][tid];
       }
+      // publish this level's last row for the warp below, then update rows
+      // R-1 .. 1 (their y-1 neighbour is the thread's own previous row) while
+      // the other warps catch up, and row 0 after the barrier
       s_row[parity][warp][lane] = cur[R - 1];
-      __syncthreads();
-      const int64_t up0 = (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0];
-      parity ^= 1;
       // x-1 neighbour; lane 0 (the tile's halo column) receives its own value
       int64_t left[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
-#pragma unroll
-      for (int r = R - 1; r >= 0; --r) {
+      auto row = [&](int r, int64_t upv) {
         const int64_t c = cur[r];
-        const int64_t upv = (r > 0) ? cur[r - 1] : up0;
         const int64_t nv = update(c, HSM ? zb[r] : hist[HSM ? 0 : t][r], upv, left[r], a);
         if (HSM)
           s_hist[t][r][tid] = c;
         else
           hist[HSM ? 0 : t][r] = c;
         cur[r] = nv;
-      }
+      };
+#pragma unroll
+      for (int r = R - 1; r >= 1; --r) row(r, cur[r - 1]);
+      __syncthreads();
+      row(0, (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0]);
+      parity ^= 1;
     }
     if (p >= K) {
       int64_t* dst = out + po;
