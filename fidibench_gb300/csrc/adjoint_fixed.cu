@@ -8,18 +8,22 @@
 // <lam', S_j f - f> and the periodic shift invariance, so f is read only at
 // i).  The lam update is the forward fixed-point update with every axis
 // flipped, so the kernel reuses its update and scale ring (step_fixed.cuh)
-// with one step per launch: 24 B of HBM per cell-step (lam in and out, f^n
-// in), the differences D_j shared between the update and the contraction.
-// The contraction D_j * F^n is a 64x64 product rounded to 2^64 units (three
-// IMAD.WIDE on balanced 32-bit halves), summed per thread in int64 per plane
-// and in a 128-bit integer across planes; each CTA adds its three sums into
-// its own slot of a per-call array (fixed CTA -> tile map, so the result is
+// with one step per launch: 20 B of HBM per cell-step (lam in and out, f^n
+// in as int32), the differences D_j shared between the update and the
+// contraction.  The contraction takes F^n rounded to 2^29 units (G, int32,
+// 2^-30 of the 2^59 range) and D_j whole: D_j * G / 2^32 from two IMAD.WIDE
+// on D's balanced halves, summed per thread in int64 over four planes and in
+// a 128-bit integer across planes; each CTA adds its three sums into its own
+// slot of a per-call array (fixed CTA -> tile map, so the result is
 // deterministic).
 //
-// Forward states f^n of a checkpoint segment are recomputed by the forward
-// fixed kernel with one step per launch into int64 buffers; each launch logs
-// its output scale on the device, which the adjoint launch for that step
-// reads.  Elementwise kernels convert FP64 <-> int64 at the ends.
+// Forward states f^n of a checkpoint segment are recomputed with one step
+// per launch by the same kernel without the transpose and the contraction:
+// the int64 chain goes through two ping-pong buffers and each state is also
+// stored rounded to 2^29 units (int32, one array per step of the segment).
+// Each launch logs its output scale on the device, which the adjoint launch
+// for that step reads.  Elementwise kernels convert FP64 <-> int64 at the
+// ends.
 #include <math.h>
 
 #include <algorithm>
@@ -37,6 +41,16 @@ namespace {
 
 constexpr int kAR = 4;  // rows per thread
 constexpr int kAW = 8;  // warps per CTA
+constexpr int kAMinBlocks = 3;  // resident CTAs per SM the registers are sized for
+
+// The contraction reads a state F as G = F / 2^kGShift rounded: every
+// launch's output has |F| < 2^59 (scale_from_slot puts the input below
+// 2^(59 - guard); the guard bits cover the step's growth; one step's
+// rounding adds at most 8 units), so |G| <= 2^30 fits int32.
+constexpr int kGShift = 29;
+__device__ __forceinline__ int32_t state_round(int64_t v) {
+  return (int32_t)((v + (1ll << (kGShift - 1))) >> kGShift);
+}
 
 // v = hi 2^32 + lo with both halves signed (lo in [-2^31, 2^31))
 __device__ __forceinline__ void split_balanced(int64_t v, int32_t* hi, int32_t* lo) {
@@ -44,13 +58,14 @@ __device__ __forceinline__ void split_balanced(int64_t v, int32_t* hi, int32_t* 
   *hi = (int32_t)(v >> 32) + (int32_t)((uint32_t)v >> 31);
 }
 
-// round(D * F / 2^64) from balanced halves (|D| < 2^62, |F| < 2^61): the two
-// cross products (|.| <= 2^61 and 2^60) sum exactly in int64
-__device__ __forceinline__ int64_t prod64(int64_t D, int32_t g1, int32_t g0) {
+// Contraction term D G / 2^32 = D F / 2^(32 + kGShift), D whole: the high
+// half of D times G plus the low half's product rounded (two IMAD.WIDE).
+// |D| < 2^60 (its high half <= 2^28) and |G| <= 2^30 bound the term by
+// 2^58 + 2^29.  D = 0 gives 0 exactly, so zero regions add nothing.
+__device__ __forceinline__ int64_t dot_term(int64_t D, int32_t G) {
   int32_t d1, d0;
   split_balanced(D, &d1, &d0);
-  const int64_t t = mulw_s(d1, g0) + mulw_s(d0, g1) + 0x80000000ll;
-  return mulw_s(d1, g1) + (t >> 32);
+  return mulw_s(d1, G) + ((mulw_s(d0, G) + 0x80000000ll) >> 32);
 }
 
 // 128-bit accumulator of signed int64 terms
@@ -93,31 +108,38 @@ __device__ __forceinline__ double pow2(int e) {
 // Each plane of the input is staged by cp.async into shared memory with its
 // upstream halo (row 0 = the y-1 row, column 0 = the x-1 column), so every
 // neighbour of a cell is one shared-memory load: no shuffles, no selects,
-// one __syncthreads per plane.  Three input planes rotate (z-1, z, and the
-// one being fetched); the forward state F^n (DOTS) is staged the same way.
+// one __syncthreads per plane.  kAhead planes are in flight while one is
+// computed, so kNL = kAhead + 2 input planes rotate (z-1, z and the ones
+// being fetched); the forward state F^n (DOTS, int32 in 2^29 units) is
+// staged the same way in kNF = kAhead + 1 buffers.  Without DOTS (the
+// forward recompute) each output value is also stored rounded to 2^29
+// units in out_hi, the form the contraction reads.
 // Thread (warp w, lane l) owns cells (x = l, y = w*R + r) of the tile.
+constexpr int kAhead = 2;
+constexpr int kNL = kAhead + 2;
+constexpr int kNF = kAhead + 1;
 template <int R, int W, bool DOTS>
 struct AdjTileSmem {
   static constexpr int kRows = R * W;              // tile rows (32)
   static constexpr int kLRow = 33;                 // halo column + 32 cells
   static constexpr int kLPlane = (kRows + 1) * kLRow;
   static constexpr int kFPlane = kRows * 32;
-  static constexpr int bytes() { return (3 * kLPlane + (DOTS ? 2 * kFPlane : 0)) * 8; }
+  static constexpr int bytes() { return kNL * kLPlane * 8 + (DOTS ? kNF * kFPlane * 4 : 0); }
 };
 
 template <int R, int W, bool DOTS>
-__global__ void __launch_bounds__(32 * W, 3)
+__global__ void __launch_bounds__(32 * W, kAMinBlocks)
 k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
-               const int64_t* __restrict__ fstate, const int* __restrict__ fscale,
-               const FixedArgs a, double* __restrict__ dpart) {
+               int32_t* __restrict__ out_hi, const int32_t* __restrict__ fstate,
+               const int* __restrict__ fscale, const FixedArgs a, double* __restrict__ dpart) {
   using SM = AdjTileSmem<R, W, DOTS>;
   static_assert(SM::kRows == 32, "the halo column is loaded by one warp");
   extern __shared__ __align__(16) int64_t s_dyn[];
   __shared__ unsigned long long s_or[W];
   __shared__ unsigned long long s_red_lo[3][W];
   __shared__ long long s_red_hi[3][W];
-  int64_t* sL = s_dyn;                  // [3][kRows + 1][33]
-  int64_t* sF = s_dyn + 3 * SM::kLPlane;  // [2][kRows][32]
+  int64_t* sL = s_dyn;                                  // [kNL][kRows + 1][33]
+  int32_t* sF = (int32_t*)(s_dyn + kNL * SM::kLPlane);  // [kNF][kRows][32]
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -173,22 +195,29 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
     return sL + buf * SM::kLPlane + row * SM::kLRow + col;
   };
 
-  // fetch plane j (j = 0: z = Z0-1, the z-1 history of the first plane)
-  // fetch a plane (physical offset po) into lambda buffer b and, with f, into
-  // f buffer fb
-  auto fetch = [&](int b, int64_t po, bool with_f, int fb) {
+  // this thread's cells in lambda buffer 0 (row 1 + warp*R, column 1 + lane)
+  // and in F buffer 0, and its in-plane element offsets (ny * nx < 2^31)
+  int64_t* const myl = sL + (1 + warp * R) * SM::kLRow + 1 + lane;
+  int32_t* const myf = sF + warp * R * 32 + lane;
+  int gofs[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r)
-      fx::cp_async8(lam_at(b, 1 + warp * R + r, 1 + lane), in + po + roff[r] + px);
+  for (int r = 0; r < R; ++r) gofs[r] = roff[r] + px;
+  // fetch a plane (physical offset po) into lambda buffer b and, with_f, its
+  // state into F buffer fb
+  auto fetch = [&](int b, int64_t po, bool with_f, int fb) {
+    const int64_t* pin = in + po;
+    int64_t* l = myl + b * SM::kLPlane;
+#pragma unroll
+    for (int r = 0; r < R; ++r) fx::cp_async8(l + r * SM::kLRow, pin + gofs[r]);
     if (warp == 0) {
-      fx::cp_async8(lam_at(b, 0, 1 + lane), in + po + rhalo);
-      fx::cp_async8(lam_at(b, 1 + lane, 0), in + po + chalo);
+      fx::cp_async8(lam_at(b, 0, 1 + lane), pin + rhalo);
+      fx::cp_async8(lam_at(b, 1 + lane, 0), pin + chalo);
     }
     if (DOTS && with_f) {
+      const int32_t* pf = fstate + po;
+      int32_t* f = myf + fb * SM::kFPlane;
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-        fx::cp_async8(sF + fb * SM::kFPlane + (warp * R + r) * 32 + lane,
-                      fstate + po + roff[r] + px);
+      for (int r = 0; r < R; ++r) fx::cp_async4(f + r * 32, pf + gofs[r]);
     }
     fx::cp_async_commit();
   };
@@ -203,33 +232,36 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
     }
   };
 
-  // The contraction terms are below 2^55 (|D| < 2^60, |F| < 2^59): int64
-  // sums take 32 planes of R = 4 rows before they go into the 128-bit ones.
+  // The contraction terms are below 2^58 + 2^29: int64 sums take 4 planes
+  // of R = 4 rows before they go into the 128-bit ones.
   Acc128 acc[3];
   int64_t part[3] = {0, 0, 0};
   unsigned long long my_or = 0ull;
   // one plane: lambda buffers b (z) and bm (z-1), f buffer fb, output at po
   auto compute = [&](auto full_tag, int b, int bm, int fb, int64_t po) {
     constexpr bool kFull = decltype(full_tag)::value;
-    int64_t* dst = out + po + px;
+    int64_t* dst = out + po;
+    int32_t* dst_hi = DOTS ? nullptr : out_hi + po;
+    const int64_t* l = myl + b * SM::kLPlane;
+    const int64_t* lm = myl + bm * SM::kLPlane;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int row = 1 + warp * R + r;
-      const int64_t c = *lam_at(b, row, 1 + lane);
-      const int64_t Dz = *lam_at(bm, row, 1 + lane) - c;
-      const int64_t Dy = *lam_at(b, row - 1, 1 + lane) - c;
-      const int64_t Dx = *lam_at(b, row, lane) - c;
+      const int64_t c = l[r * SM::kLRow];
+      const int64_t Dz = lm[r * SM::kLRow] - c;
+      const int64_t Dy = l[r * SM::kLRow - SM::kLRow] - c;
+      const int64_t Dx = l[r * SM::kLRow - 1] - c;
       const int64_t nv = fixed_update_d(c, Dz, Dy, Dx, a.qz, a.qy, a.qx);
       if (kFull || (row_mask & (1u << r))) {
         if (DOTS) {
-          int32_t g1, g0;
-          split_balanced(sF[fb * SM::kFPlane + (warp * R + r) * 32 + lane], &g1, &g0);
-          part[0] += prod64(Dz, g1, g0);
-          part[1] += prod64(Dy, g1, g0);
-          part[2] += prod64(Dx, g1, g0);
+          const int32_t G = myf[fb * SM::kFPlane + r * 32];
+          part[0] += dot_term(Dz, G);
+          part[1] += dot_term(Dy, G);
+          part[2] += dot_term(Dx, G);
+        } else {
+          dst_hi[gofs[r]] = state_round(nv);
         }
         my_or |= (unsigned long long)(nv ^ (nv >> 63));
-        dst[roff[r]] = nv;
+        dst[gofs[r]] = nv;
       }
     }
   };
@@ -238,26 +270,45 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
   const int64_t dz = a.fz ? -plane_sz : plane_sz;
   const int64_t wrap_po = a.fz ? (int64_t)(a.nz - 1) * plane_sz : 0;
 
-  int lz = fx::wrap_mod(Z0 - 1, a.nz);
-  int64_t po = plane_off(lz);
-  int b = 0;  // lambda buffer of plane j (j mod 3)
-  fetch(0, po, false, 0);
-  for (int j = 0; j <= nz_tile; ++j) {
-    fx::cp_async_wait<0>();
-    if (d != 0) rescale(b);
-    __syncthreads();
+  // plane j (j = 0: z = Z0 - 1, the z-1 history of the first output plane)
+  // goes to lambda buffer j % kNL and its state to F buffer j % kNF; planes
+  // j + 1 .. j + kAhead are in flight while plane j is computed.  Every
+  // iteration commits one cp.async group (empty past the last plane), so
+  // waiting for all but the kAhead - 1 newest groups completes plane j.
+  auto advance = [&](int& lz, int64_t& po) {
     const bool wraps = lz + 1 == a.nz;
     lz = wraps ? 0 : lz + 1;
-    const int64_t po_next = wraps ? wrap_po : po + dz;
-    const int bn = b == 2 ? 0 : b + 1;
-    if (j < nz_tile) fetch(bn, po_next, true, (j + 1) & 1);
+    po = wraps ? wrap_po : po + dz;
+  };
+  int lz = fx::wrap_mod(Z0 - 1, a.nz);  // plane j
+  int64_t po = plane_off(lz);
+  int lz_f = lz;  // the next plane to fetch
+  int64_t po_f = po;
+#pragma unroll
+  for (int k = 0; k < kAhead; ++k) {
+    if (k <= nz_tile) fetch(k, po_f, k > 0, k % kNF);
+    else fx::cp_async_commit();
+    advance(lz_f, po_f);
+  }
+  int b = 0, fb = 0;  // buffers of plane j
+  for (int j = 0; j <= nz_tile; ++j) {
+    fx::cp_async_wait<kAhead - 1>();
+    if (d != 0) rescale(b);
+    __syncthreads();
+    // the buffers of plane j + kAhead held plane j + kAhead - kNL (lambda)
+    // and j + kAhead - kNF (F), last read in iteration j - 1
+    const int bf = b + kAhead >= kNL ? b + kAhead - kNL : b + kAhead;
+    const int fbf = fb + kAhead >= kNF ? fb + kAhead - kNF : fb + kAhead;
+    if (j + kAhead <= nz_tile) fetch(bf, po_f, true, fbf);
+    else fx::cp_async_commit();
+    advance(lz_f, po_f);
     if (j > 0) {
-      const int bm = b == 0 ? 2 : b - 1;
+      const int bm = b == 0 ? kNL - 1 : b - 1;
       if (full)
-        compute(std::true_type{}, b, bm, j & 1, po);
+        compute(std::true_type{}, b, bm, fb, po);
       else
-        compute(std::false_type{}, b, bm, j & 1, po);
-      if (DOTS && (j & 31) == 0) {
+        compute(std::false_type{}, b, bm, fb, po);
+      if (DOTS && (j & 3) == 0) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           acc[k].add(part[k]);
@@ -265,8 +316,9 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
         }
       }
     }
-    b = bn;
-    po = po_next;
+    b = b + 1 == kNL ? 0 : b + 1;
+    fb = fb + 1 == kNF ? 0 : fb + 1;
+    advance(lz, po);
   }
   if (DOTS) {
 #pragma unroll
@@ -274,7 +326,7 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
   }
 
   // CTA sums of the three contractions (exact integers in units of
-  // 2^(64 - s - sf)); one FP64 conversion per sum and CTA
+  // 2^(32 + kGShift - s - sf)); one FP64 conversion per sum and CTA
   if (DOTS) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -294,17 +346,17 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
       u.hi = s_red_hi[tid][w];
       t.add(u);
     }
-    dpart[3 * blockIdx.x + tid] += t.to_double() * pow2(64 - s - sf);
+    dpart[3 * blockIdx.x + tid] += t.to_double() * pow2(32 + kGShift - s - sf);
   }
 }
 
 // f (FP64) -> F (int64) with the scale of a kind-0 slot (max|f| pre-pass);
 // writes the output slot (OR of |F|, scale, kind 1), clears the next one and
-// logs the scale.
+// logs the scale.  F_hi (nullable) receives F rounded to 2^29 units.
 __global__ void __launch_bounds__(256)
-k_to_fixed(const double* __restrict__ f, int64_t* __restrict__ F, uint64_t n,
-           const ScaleSlot* slot_in, ScaleSlot* slot_out, ScaleSlot* slot_reset, int guard,
-           int* scale_log, int* err) {
+k_to_fixed(const double* __restrict__ f, int64_t* __restrict__ F, int32_t* __restrict__ F_hi,
+           uint64_t n, const ScaleSlot* slot_in, ScaleSlot* slot_out, ScaleSlot* slot_reset,
+           int guard, int* scale_log, int* err) {
   __shared__ unsigned long long s_or[8];
   int s, d;
   if (!fx::scale_from_slot(slot_in, guard, &s, &d) && threadIdx.x == 0) atomicOr(err, 1);
@@ -319,6 +371,7 @@ k_to_fixed(const double* __restrict__ f, int64_t* __restrict__ F, uint64_t n,
   for (uint64_t i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (uint64_t)gridDim.x * 256ull) {
     const int64_t v = to_fixed(__ldg(f + i), s);
     F[i] = v;
+    if (F_hi) F_hi[i] = state_round(v);
     my_or |= (unsigned long long)(v ^ (v >> 63));
   }
   fx::cta_or<8>(my_or, s_or, &slot_out->m);
@@ -402,11 +455,24 @@ size_t adjoint_fixed_scratch_bytes(int seg_len) {
   return 6 * sizeof(ScaleSlot) + 4 * sizeof(int) + (size_t)(seg_len + 1) * sizeof(int);
 }
 
+// Dynamic shared memory above the 48 KB default needs an opt-in per kernel
+// (and device): set it for both forms before any launch.
+static int set_smem_limits() {
+  FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile<kAR, kAW, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    AdjTileSmem<kAR, kAW, true>::bytes()));
+  FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile<kAR, kAW, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    AdjTileSmem<kAR, kAW, false>::bytes()));
+  return FDB_OK;
+}
+
 // CTAs of the one-step kernel that fit on the current GPU at once.
 static int64_t step1_resident() {
   static int per_sm = -1;  // benign race (idempotent)
   if (per_sm < 0) {
     int occ = 0;
+    set_smem_limits();
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint_tile<kAR, kAW, true>,
                                                       32 * kAW,
                                                       AdjTileSmem<kAR, kAW, true>::bytes()) !=
@@ -452,6 +518,7 @@ int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c) {
 }
 
 int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
+  FDB_TRY(set_smem_limits());
   const Geom& g = *io.g;
   const Coeffs3& c = *io.c;
   const uint64_t n = g.ntot;
@@ -471,8 +538,8 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   FDB_CUDA_TRY(cudaMemsetAsync(io.dpart, 0, 3 * sizeof(double) * nblk, st));
   k_ring_init<<<1, 32, 0, st>>>(lr);
   k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.lam_T, n, lr);
-  k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.lam_T, io.lam[0], n, lr, lr + 1, lr + 2, gK, nullptr,
-                                         err);
+  k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.lam_T, io.lam[0], nullptr, n, lr, lr + 1, lr + 2,
+                                         gK, nullptr, err);
   note_launch(3);
   int li = 1;  // adjoint ring position of the next launch
   int lc = 0;
@@ -485,11 +552,12 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       cudaEventCreate(&e2);
       cudaEventRecord(e0, st);
     }
-    // states f^{sK} .. f^{sK+len-1} in int64 (forward ring, launch index 0..len-1)
+    // states f^{sK} .. f^{sK+len-1} (forward ring, launch index 0..len-1):
+    // state k in int64 in chain[k & 1], rounded to 2^29 units in state_hi[k]
     k_ring_init<<<1, 32, 0, st>>>(fr);
     k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], n, fr);
-    k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.states[0], n, fr, fr + 1, fr + 2, gK,
-                                           logs + 0, err);
+    k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], n, fr,
+                                           fr + 1, fr + 2, gK, logs + 0, err);
     note_launch(3);
     for (int k = 1; k < len; ++k) {
       aF.slot_in = fr + (k % 3);
@@ -498,7 +566,8 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aF.scale_log = logs + k;
       k_adjoint_tile<kAR, kAW, false>
           <<<nblk, 32 * kAW, AdjTileSmem<kAR, kAW, false>::bytes(), st>>>(
-          io.states[k - 1], io.states[k], nullptr, nullptr, aF, nullptr);
+              io.chain[(k - 1) & 1], io.chain[k & 1], io.state_hi[k], nullptr, nullptr, aF,
+              nullptr);
       note_launch();
     }
     FDB_CUDA_TRY(cudaGetLastError());
@@ -513,7 +582,7 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aT.slot_reset = lr + ((li + 2) % 3);
       k_adjoint_tile<kAR, kAW, true>
           <<<nblk, 32 * kAW, AdjTileSmem<kAR, kAW, true>::bytes(), st>>>(
-              io.lam[lc], io.lam[lc ^ 1], io.states[k], logs + k, aT, io.dpart);
+              io.lam[lc], io.lam[lc ^ 1], nullptr, io.state_hi[k], logs + k, aT, io.dpart);
       note_launch();
       FDB_CUDA_TRY(cudaGetLastError());
       lc ^= 1;

@@ -461,11 +461,14 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   const int arith = fixed ? FDB_ARITH_FIXED
                           : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
 
-  // storage: nseg checkpoints, K segment states, two adjoint buffers
-  if ((int)h->ckpt.size() < nseg || (int)h->seg.size() < K || !h->lam[0]) {
+  // storage: nseg checkpoints, the segment's states (FP64: K - 1 buffers;
+  // fixed point: two int64 chain buffers and K int32 arrays), two adjoint
+  // buffers
+  const int nsegbuf = std::max(K, adjoint_fixed_segment_buffers(K));
+  if ((int)h->ckpt.size() < nseg || (int)h->seg.size() < nsegbuf || !h->lam[0]) {
     free_adjoint(h);
     h->ckpt.assign(nseg, nullptr);
-    h->seg.assign(K, nullptr);
+    h->seg.assign(nsegbuf, nullptr);
     int rc = FDB_OK;
     for (auto& p : h->ckpt)
       if (!rc) rc = dalloc(&p, g.ntot);
@@ -542,7 +545,11 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     io.K = K;
     io.nseg = nseg;
     io.ckpt = h->ckpt.data();
-    io.states = (int64_t* const*)h->seg.data();
+    io.chain[0] = (int64_t*)h->seg[0];
+    io.chain[1] = (int64_t*)h->seg[1];
+    std::vector<int32_t*> hi(K);
+    for (int k = 0; k < K; ++k) hi[k] = (int32_t*)h->seg[2 + k / 2] + (k & 1) * g.ntot;
+    io.state_hi = hi.data();
     io.lam[0] = (int64_t*)h->lam[0];
     io.lam[1] = (int64_t*)h->lam[1];
     io.lam_T = lamT;

@@ -127,7 +127,11 @@ struct AdjointFixedIO {
   int K;      // checkpoint interval
   int nseg;   // ceil(S / K)
   double* const* ckpt;
-  int64_t* const* states;  // K int64 buffers for one recomputed segment
+  // recomputed segment: its states march through two int64 buffers; the
+  // contraction reads each state's values rounded to 2^32 units, kept as
+  // int32 (K arrays of ntot)
+  int64_t* chain[2];
+  int32_t* const* state_hi;
   int64_t* lam[2];         // adjoint ping-pong (int64)
   const double* lam_T;     // device, FP64
   double* grad_f0;         // device, FP64
@@ -141,6 +145,9 @@ struct AdjointFixedIO {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* adjoint_ev = nullptr;
 };
 size_t adjoint_fixed_scratch_bytes(int seg_len);
+// ntot-double buffers the fixed-point adjoint needs for a segment of K steps:
+// the two int64 chain buffers and K int32 arrays (two per buffer)
+inline int adjoint_fixed_segment_buffers(int K) { return 2 + (K + 1) / 2; }
 int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c);
 int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st);
 
