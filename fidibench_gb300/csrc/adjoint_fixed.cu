@@ -10,17 +10,17 @@
 // flipped, so the kernel reuses its update and scale ring (step_fixed.cuh)
 // with one step per launch: 20 B of HBM per cell-step (lam in and out, f^n
 // in as int32), the differences D_j shared between the update and the
-// contraction.  The contraction takes F^n rounded to 2^29 units (G, int32,
-// 2^-30 of the 2^59 range) and D_j whole: D_j * G / 2^32 from two IMAD.WIDE
-// on D's balanced halves, summed per thread in int64 over four planes and in
-// a 128-bit integer across planes; each CTA adds its three sums into its own
-// slot of a per-call array (fixed CTA -> tile map, so the result is
-// deterministic).
+// contraction.  The contraction takes F^n in 2^29 units (G, int32,
+// 2^-30 of the 2^59 range) and D_j whole: D_j * G / 2^32 from the update's
+// own split of D (high word times G by IMAD.WIDE, low word by IMAD.HI),
+// summed per thread in int64 over four planes and in a 128-bit integer
+// across planes; each CTA adds its three sums into its own slot of a
+// per-call array (fixed CTA -> tile map, so the result is deterministic).
 //
 // Forward states f^n of a checkpoint segment are recomputed with one step
 // per launch by the same kernel without the transpose and the contraction:
 // the int64 chain goes through two ping-pong buffers and each state is also
-// stored rounded to 2^29 units (int32, one array per step of the segment).
+// stored in 2^29 units (int32, one array per step of the segment).
 // Each launch logs its output scale on the device, which the adjoint launch
 // for that step reads.  Elementwise kernels convert FP64 <-> int64 at the
 // ends.
@@ -43,29 +43,32 @@ constexpr int kAR = 4;  // rows per thread
 constexpr int kAW = 8;  // warps per CTA
 constexpr int kAMinBlocks = 3;  // resident CTAs per SM the registers are sized for
 
-// The contraction reads a state F as G = F / 2^kGShift rounded: every
+// The contraction reads a state F as G = floor(F / 2^kGShift): every
 // launch's output has |F| < 2^59 (scale_from_slot puts the input below
 // 2^(59 - guard); the guard bits cover the step's growth; one step's
-// rounding adds at most 8 units), so |G| <= 2^30 fits int32.
+// rounding adds at most 8 units), so |G| <= 2^30 fits int32.  Flooring
+// rather than rounding shifts G by half a unit on average, and a constant
+// shift adds nothing: sum_i D_j[i] = 0 over the periodic grid.
 constexpr int kGShift = 29;
-__device__ __forceinline__ int32_t state_round(int64_t v) {
-  return (int32_t)((v + (1ll << (kGShift - 1))) >> kGShift);
+__device__ __forceinline__ int32_t state_g(int64_t v) {
+  return (int32_t)(v >> kGShift);
 }
 
-// v = hi 2^32 + lo with both halves signed (lo in [-2^31, 2^31))
-__device__ __forceinline__ void split_balanced(int64_t v, int32_t* hi, int32_t* lo) {
-  *lo = (int32_t)(uint32_t)v;
-  *hi = (int32_t)(v >> 32) + (int32_t)((uint32_t)v >> 31);
+// floor(a * b / 2^32) (one IMAD.HI)
+__device__ __forceinline__ int32_t mulhi_s(int32_t a, int32_t b) {
+  int32_t d;
+  asm("mul.hi.s32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
 }
 
-// Contraction term D G / 2^32 = D F / 2^(32 + kGShift), D whole: the high
-// half of D times G plus the low half's product rounded (two IMAD.WIDE).
-// |D| < 2^60 (its high half <= 2^28) and |G| <= 2^30 bound the term by
-// 2^58 + 2^29.  D = 0 gives 0 exactly, so zero regions add nothing.
-__device__ __forceinline__ int64_t dot_term(int64_t D, int32_t G) {
-  int32_t d1, d0;
-  split_balanced(D, &d1, &d0);
-  return mulw_s(d1, G) + ((mulw_s(d0, G) + 0x80000000ll) >> 32);
+// One contraction term D G / 2^32 = D F / 2^(32 + kGShift), from D's high
+// word d1 and low word d0 (D = d1 2^32 + d0, the split the update uses):
+// d1 G (exact, |.| <= 2^58) into p, and floor((d0 >> 1) G / 2^32) (within
+// 1 of d0 G / 2^33, |.| <= 2^29) into q, which the caller adds to p as 2 q
+// after at most four terms (|q| <= 2^31 still fits int32).  D = 0 adds 0.
+__device__ __forceinline__ void dot_term(int64_t D, int32_t G, int64_t& p, int32_t& q) {
+  p += mulw_s((int32_t)(D >> 32), G);
+  q += mulhi_s((int32_t)((uint32_t)D >> 1), G);
 }
 
 // 128-bit accumulator of signed int64 terms
@@ -112,8 +115,8 @@ __device__ __forceinline__ double pow2(int e) {
 // computed, so kNL = kAhead + 2 input planes rotate (z-1, z and the ones
 // being fetched); the forward state F^n (DOTS, int32 in 2^29 units) is
 // staged the same way in kNF = kAhead + 1 buffers.  Without DOTS (the
-// forward recompute) each output value is also stored rounded to 2^29
-// units in out_hi, the form the contraction reads.
+// forward recompute) each output value is also stored in 2^29 units in
+// out_hi, the form the contraction reads.
 // Thread (warp w, lane l) owns cells (x = l, y = w*R + r) of the tile.
 constexpr int kAhead = 2;
 constexpr int kNL = kAhead + 2;
@@ -232,8 +235,10 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
     }
   };
 
-  // The contraction terms are below 2^58 + 2^29: int64 sums take 4 planes
-  // of R = 4 rows before they go into the 128-bit ones.
+  // dot_term: per plane at most R = 4 terms in q; per 4 planes 16 terms
+  // (|.| <= 2^58) and 4 folds (|2 q| <= 2^32) in the int64 sums before they
+  // go into the 128-bit ones.
+  static_assert(R <= 4, "q holds at most four terms");
   Acc128 acc[3];
   int64_t part[3] = {0, 0, 0};
   unsigned long long my_or = 0ull;
@@ -244,6 +249,7 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
     int32_t* dst_hi = DOTS ? nullptr : out_hi + po;
     const int64_t* l = myl + b * SM::kLPlane;
     const int64_t* lm = myl + bm * SM::kLPlane;
+    int32_t q[3] = {0, 0, 0};
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int64_t c = l[r * SM::kLRow];
@@ -254,15 +260,19 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
       if (kFull || (row_mask & (1u << r))) {
         if (DOTS) {
           const int32_t G = myf[fb * SM::kFPlane + r * 32];
-          part[0] += dot_term(Dz, G);
-          part[1] += dot_term(Dy, G);
-          part[2] += dot_term(Dx, G);
+          dot_term(Dz, G, part[0], q[0]);
+          dot_term(Dy, G, part[1], q[1]);
+          dot_term(Dx, G, part[2], q[2]);
         } else {
-          dst_hi[gofs[r]] = state_round(nv);
+          dst_hi[gofs[r]] = state_g(nv);
         }
         my_or |= (unsigned long long)(nv ^ (nv >> 63));
         dst[gofs[r]] = nv;
       }
+    }
+    if (DOTS) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) part[k] += 2 * (int64_t)q[k];
     }
   };
   // the tile lies inside the grid: every thread stores all R rows
@@ -352,7 +362,7 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
 
 // f (FP64) -> F (int64) with the scale of a kind-0 slot (max|f| pre-pass);
 // writes the output slot (OR of |F|, scale, kind 1), clears the next one and
-// logs the scale.  F_hi (nullable) receives F rounded to 2^29 units.
+// logs the scale.  F_hi (nullable) receives F in 2^29 units.
 __global__ void __launch_bounds__(256)
 k_to_fixed(const double* __restrict__ f, int64_t* __restrict__ F, int32_t* __restrict__ F_hi,
            uint64_t n, const ScaleSlot* slot_in, ScaleSlot* slot_out, ScaleSlot* slot_reset,
@@ -371,7 +381,7 @@ k_to_fixed(const double* __restrict__ f, int64_t* __restrict__ F, int32_t* __res
   for (uint64_t i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (uint64_t)gridDim.x * 256ull) {
     const int64_t v = to_fixed(__ldg(f + i), s);
     F[i] = v;
-    if (F_hi) F_hi[i] = state_round(v);
+    if (F_hi) F_hi[i] = state_g(v);
     my_or |= (unsigned long long)(v ^ (v >> 63));
   }
   fx::cta_or<8>(my_or, s_or, &slot_out->m);
@@ -473,13 +483,9 @@ static int64_t step1_resident() {
   if (per_sm < 0) {
     int occ = 0;
     set_smem_limits();
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint_tile<kAR, kAW, true>,
-                                                      32 * kAW,
-                                                      AdjTileSmem<kAR, kAW, true>::bytes()) !=
-            cudaSuccess ||
-        occ < 1)
-      occ = 1;
-    per_sm = occ;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, k_adjoint_tile<kAR, kAW, true>, 32 * kAW, AdjTileSmem<kAR, kAW, true>::bytes());
+    per_sm = (e != cudaSuccess || occ < 1) ? 1 : occ;
   }
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -487,11 +493,11 @@ static int64_t step1_resident() {
   return (int64_t)per_sm * (sms > 0 ? sms : 1);
 }
 
-// Tiling of the one-step kernel: 32 columns x (kAR*kAW) rows per CTA and
-// as many z-slabs as fill one wave of resident CTAs (long z-runs amortise
-// each CTA's set-up, warm-up plane and final reduction; one wave has no
-// partial last wave), at least 4 planes each.
-// transpose = true: the adjoint (every upwind direction reversed).
+// Tiling of the one-step kernel: 32 columns x (kAR*kAW) rows per CTA and as
+// many z-slabs as fill one wave of resident CTAs (long z-runs amortise each
+// CTA's set-up, warm-up planes and final reduction; one wave has no partial
+// last wave), at least 4 planes each.  transpose = true: the adjoint (every
+// upwind direction reversed).
 static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
   FixedArgs a = make_fixed_args(transpose ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
                                 (int64_t)2 * 152);
@@ -512,9 +518,10 @@ static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
   return a;
 }
 
+static int grid_of(const FixedArgs& a) { return a.tiles_x * a.tiles_y * a.tiles_z; }
+
 int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c) {
-  const FixedArgs a = step1_args(g, c, true);
-  return a.tiles_x * a.tiles_y * a.tiles_z;
+  return grid_of(step1_args(g, c, true));
 }
 
 int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
@@ -531,7 +538,7 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   aT.err = err;
   FixedArgs aF = step1_args(g, c, false);
   aF.err = err;
-  const int nblk = aT.tiles_x * aT.tiles_y * aT.tiles_z;
+  const int nblk = grid_of(aT), nblkF = grid_of(aF);
   if (nblk > io.dpart_cap) return fail(FDB_ERR_INVALID, "adjoint partial-sum buffer too small");
 
   // lam_T -> int64 (adjoint ring, launch index 0)
@@ -553,7 +560,7 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       cudaEventRecord(e0, st);
     }
     // states f^{sK} .. f^{sK+len-1} (forward ring, launch index 0..len-1):
-    // state k in int64 in chain[k & 1], rounded to 2^29 units in state_hi[k]
+    // state k in int64 in chain[k & 1], in 2^29 units in state_hi[k]
     k_ring_init<<<1, 32, 0, st>>>(fr);
     k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], n, fr);
     k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], n, fr,
@@ -565,7 +572,7 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       aF.slot_reset = fr + ((k + 2) % 3);
       aF.scale_log = logs + k;
       k_adjoint_tile<kAR, kAW, false>
-          <<<nblk, 32 * kAW, AdjTileSmem<kAR, kAW, false>::bytes(), st>>>(
+          <<<nblkF, 32 * kAW, AdjTileSmem<kAR, kAW, false>::bytes(), st>>>(
               io.chain[(k - 1) & 1], io.chain[k & 1], io.state_hi[k], nullptr, nullptr, aF,
               nullptr);
       note_launch();

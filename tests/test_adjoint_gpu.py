@@ -109,7 +109,7 @@ def test_finite_differences(fdb, port, arith):
 def test_fixed_adjoint_matches_fp64_adjoint(fdb, v):
     """The two adjoint arithmetics agree: dL/df0 to 1e-12 of max|grad|; the
     velocity gradients to 1e-8, since the fixed-point contraction reads each
-    forward state rounded to 2^29 units (2^-30 of the fixed-point range), an
+    forward state in 2^29 units (2^-30 of the fixed-point range), an
     error that for random fields is below 1e-9 of the contraction."""
     n, L = (20, 28, 36), (1.0, 1.0, 1.0)
     steps, dt = 45, 0.45 / 36
