@@ -485,20 +485,23 @@ int run_batched(fdb_batch* b, int steps, const double* dt, int K, int shape, int
   return FDB_OK;
 }
 
-// The comparator: the plain per-field kernel looped over the instances.
-// Every instance ends in the same arena (instances whose launch count has the
-// other parity are copied across).
+// The comparator: the plain per-field kernels looped over the instances,
+// K steps per fixed-point launch; K <= 0: what fdb_upwind_advect runs for
+// each instance (the fixed kernel at its default depth where it is
+// supported and preferred, the FP64 kernel otherwise).  Every instance ends
+// in the same arena: the one most instances end in; the others are copied
+// across.
 int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
   const size_t per = (fixed_scratch_bytes() + 7) / 8;
-  const int new_cur = b->cur ^ ((((steps + K - 1) / K)) & 1);
+  std::vector<int> fin(b->count);
   for (int i = 0; i < b->count; ++i) {
     const Geom& g = b->geoms[i];
     const Coeffs3 c = coeffs3(g, dt[i]);
     double* bufs[2] = {b->arena[0] + b->offsets[i], b->arena[1] + b->offsets[i]};
     int cur = b->cur;
     FixedTuning t;
-    t.depth = K;
-    if (fixed_supported(g, c, K) == FDB_OK) {
+    t.depth = K > 0 ? K : 0;
+    if (fixed_supported(g, c, t.depth) == FDB_OK && (K > 0 || fixed_preferred(g))) {
       FDB_TRY(launch_advect_fixed_ex(g, c, steps, t, bufs, &cur, b->d_plain_scratch + i * per,
                                      per * 8, nullptr, b->stream));
     } else {
@@ -507,9 +510,15 @@ int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
         cur ^= 1;
       }
     }
-    if (cur != new_cur)
-      FDB_CUDA_TRY(cudaMemcpyAsync(bufs[new_cur], bufs[cur], b->sizes[i] * 8,
-                                   cudaMemcpyDeviceToDevice, b->stream));
+    fin[i] = cur;
+  }
+  int ones = 0;
+  for (int i = 0; i < b->count; ++i) ones += fin[i];
+  const int new_cur = 2 * ones > b->count ? 1 : 0;
+  for (int i = 0; i < b->count; ++i) {
+    if (fin[i] == new_cur) continue;
+    FDB_CUDA_TRY(cudaMemcpyAsync(b->arena[new_cur] + b->offsets[i], b->arena[fin[i]] + b->offsets[i],
+                                 b->sizes[i] * 8, cudaMemcpyDeviceToDevice, b->stream));
   }
   b->cur = new_cur;
   return FDB_OK;
@@ -685,7 +694,7 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   FDB_TRY(check_dts(b, dt));
   if (num_steps == 0) return FDB_OK;
-  return run_looped(b, num_steps, dt, 4);
+  return run_looped(b, num_steps, dt, b->K);
 }
 
 int fdb_batch_checksums(fdb_batch* b, double* out) {

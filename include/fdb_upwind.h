@@ -164,7 +164,10 @@ int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
  * time blocks, per-instance dependency tracking with bounded waits; replayed
  * from a CUDA graph when called again with the same steps, dt and tuning).
  * fdb_batch_advect_looped is the comparator: the single-field kernel looped
- * over the instances.  dt holds one time step per instance.
+ * over the instances, with the depth set by FDB_TUNE_DEPTH (equal depths
+ * give bit-identical fields) or, without one, each instance's single-field
+ * default (what fdb_upwind_advect picks).  dt holds one time step per
+ * instance.
  * ------------------------------------------------------------------------- */
 typedef struct {
   int ndims;              /* 1..3 */

@@ -50,18 +50,37 @@ def test_batched_bit_identical_to_looped(fdb, depth, shape, tile_z):
     a = make_batch(fdb, specs)
     c = make_batch(fdb, specs)
     a.set_tuning(depth=depth, shape=shape, tile_z=tile_z)
+    c.set_tuning(depth=depth)  # the looped comparator takes the same time blocks
     for _ in range(2):  # the second call replays the captured graph
         a.advect(21, dts)
         c.advect_looped(21, dts)
-    # integer arithmetic: any tiling gives the same field; the looped
-    # comparator runs 4 steps per launch, so equal time blocks are bit-equal
+    # integer arithmetic: any tiling gives the same field, so equal time
+    # blocks are bit-equal
     for k in range(a.count):
-        if depth == 4:
-            assert np.array_equal(a.get_field(k), c.get_field(k)), k
-        else:
-            assert rel_maxnorm(a.get_field(k), c.get_field(k)) <= FIELD_TOL, k
+        assert np.array_equal(a.get_field(k), c.get_field(k)), k
     a.close()
     c.close()
+
+
+def test_looped_default_depth_matches_oracle(fdb, port):
+    """Without a depth the looped comparator runs every instance as
+    fdb_upwind_advect does (fixed point at its default depth, or FP64 below
+    2^18 cells): bit-identical to Upwind.advect, and within the parity
+    tolerance of the oracle."""
+    specs = small_specs(count=6, seed=17, nmin=30, nmax=110)
+    dts = [s["dt"] for s in specs]
+    b = make_batch(fdb, specs)
+    f0 = [b.get_field(k) for k in range(b.count)]
+    b.advect_looped(13, dts)
+    for k, s in enumerate(specs):
+        ref = port.advect(s["n"], s["v"], s["L"], f0[k], 13, s["dt"])
+        assert rel_maxnorm(b.get_field(k), ref) <= FIELD_TOL, k
+        up = fdb.Upwind(s["v"], s["L"], s["n"])
+        up.f = f0[k]
+        up.advect(13, s["dt"])
+        assert np.array_equal(b.get_field(k), up.f), k
+        up.close()
+    b.close()
 
 
 def test_batched_any_depth_matches_oracle(fdb, port):
