@@ -134,9 +134,10 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   const bool out_x = (lane >= K) && (X0 + lane - K < a.nx);
 
   // offset (py * nx + px) of each of this thread's rows, wrapped once here:
-  // the rows stay the same for the whole z-march
+  // the rows stay the same for the whole z-march (unsigned: each address is
+  // one 32 x 32 -> 64-bit multiply-add)
   const int ly0 = Y0 - K + warp * R;
-  int roff[R];
+  unsigned roff[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     int ly = ly0 + r;
