@@ -6,8 +6,11 @@ on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
   advect N S  : N^3 sphere + noise field, v = (1, -0.7, 0.3), dt = 0.5/N,
                 three advect calls of S steps
   batch C S   : C seeded instances with axes in [32, 160] (the benchmark's
-                generator), three batched advects of S steps (depth 4,
-                shape 4x8 with shared-memory history)
+                generator), three batched advects of S steps (depth 3,
+                shape 4x8 with shared-memory history, whole-z tiles: the
+                tuning the autotuner picks for the benchmark's batch)
+  filter N I  : 2-D N x N laplacian Filter (the reference laplacian
+                driver's stencil and index wrap), three iterate(I) calls
 """
 from __future__ import annotations
 
@@ -48,7 +51,7 @@ def batch_case(count: int, steps: int) -> float:
     b = Batch([(s["v"], s["L"], s["n"]) for s in specs])
     for k, s in enumerate(specs):
         b.init_sphere(k, s["center"], s["radius"], 0.0, 20261203 + k)
-    b.set_tuning(depth=4, shape=4, tile_z=0)
+    b.set_tuning(depth=3, shape=4, tile_z=0)
     dts = [s["dt"] for s in specs]
     for _ in range(3):
         b.advect(steps, dts)
@@ -57,8 +60,23 @@ def batch_case(count: int, steps: int) -> float:
     return cs
 
 
+def filter_case(n: int, iters: int) -> float:
+    import numpy as np
+    from fidibench_gb300.filter import Filter, laplacian_stencil
+    x = (np.arange(n, dtype=np.float64) + 0.5) / n
+    s = np.sin(2.0 * np.pi * x)
+    flt = Filter((n, n), [0.0, 0.0], [1.0, 1.0], laplacian_stencil(2))
+    flt.set_in_data(np.ascontiguousarray((s[:, None] * s[None, :]).reshape(-1)))
+    for _ in range(3):
+        flt.iterate(iters)
+    cs = flt.computeCheckSum("out")
+    flt.close()
+    return cs
+
+
 def main(argv: list[str]) -> int:
-    cases = {"adjoint": adjoint_case, "advect": advect_case, "batch": batch_case}
+    cases = {"adjoint": adjoint_case, "advect": advect_case, "batch": batch_case,
+             "filter": filter_case}
     if len(argv) != 3 or argv[0] not in cases:
         print(__doc__)
         return 2
