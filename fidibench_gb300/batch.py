@@ -60,6 +60,13 @@ class Batch:
         check(lib.fdb_batch_count(self._h, ctypes.byref(c), ctypes.byref(t)))
         return t.value
 
+    def storage_order(self, index: int) -> tuple:
+        """Stored axis order of an instance: stored axis k is axis order[k] of
+        its 3-D view (the batch marches along the axis that tiles worst)."""
+        o = (ctypes.c_int * 3)()
+        check(lib.fdb_batch_storage_order(self._h, int(index), o))
+        return tuple(o)
+
     def _dts(self, dt) -> np.ndarray:
         d = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (self.count,)))
         return d

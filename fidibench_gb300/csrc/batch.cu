@@ -17,6 +17,14 @@
 // bounded (clock64 budget): on expiry the CTA sets an error bit and leaves,
 // the others follow, and the host reports FDB_ERR_TIMEOUT.
 //
+// Storage order.  An instance's three axes may be stored permuted: the
+// marched axis (z, no tiling) is the one that wastes most on 29-cell tiles
+// and the other two are tiled.  The update sums exact integer products, so
+// the result does not depend on the order of the axes; set_field, get_field
+// and init_sphere translate between the caller's order and the stored one.
+// Instances that the single-field path advances in FP64 keep their order, so
+// the looped comparator stays bit-identical to fdb_upwind_advect for all.
+//
 // Memory.  All instances' fields live in two arenas (ping-pong by block).
 // Halo data written by other CTAs during the launch is read with L1-bypassing
 // loads (ld.global.cg); a tile's stores are fenced before its completion is
@@ -32,6 +40,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <fstream>
 #include <sstream>
@@ -205,6 +214,65 @@ __global__ void k_batch_sum_final(const double* __restrict__ part, int count, in
   out[i] = acc;
 }
 
+// One instance between the caller's axis order (the 3-D view (z, y, x) of
+// its description, extents n) and the stored order (stored axis k = view
+// axis p[k]): to_view = false writes dst in stored order from src in view
+// order, true the other way.
+__global__ void __launch_bounds__(256)
+k_permute3(const double* __restrict__ src, double* __restrict__ dst, uint64_t n0, uint64_t n1,
+           uint64_t n2, int p0, int p1, int p2, int to_view) {
+  const uint64_t n[3] = {n0, n1, n2};
+  const uint64_t e1 = n[p1], e2 = n[p2];
+  const uint64_t total = n0 * n1 * n2;
+  for (uint64_t i = blockIdx.x * 256ull + threadIdx.x; i < total; i += (uint64_t)gridDim.x * 256ull) {
+    const uint64_t c2 = i % e2;
+    const uint64_t t = i / e2;
+    const uint64_t c1 = t % e1;
+    const uint64_t c0 = t / e1;
+    uint64_t r[3];
+    r[p0] = c0;
+    r[p1] = c1;
+    r[p2] = c2;
+    const uint64_t v = (r[0] * n1 + r[1]) * n2 + r[2];
+    if (to_view)
+      dst[v] = src[i];
+    else
+      dst[i] = src[v];
+  }
+}
+
+// Extents, velocities and lengths of the 3-D view (z, y, x) of a described
+// instance (missing leading axes: extent 1, velocity 0).
+void view3(const Geom& g, uint64_t n[3], double v[3], double L[3]) {
+  const int jj[3] = {g.jz, g.jy, g.jx};
+  for (int a = 0; a < 3; ++a) {
+    const int j = jj[a];
+    n[a] = j < 0 ? 1 : g.n[j];
+    v[a] = j < 0 ? 0.0 : g.v[j];
+    L[a] = j < 0 ? 1.0 : g.L[j];
+  }
+}
+
+// Stored order of an instance with view extents n: the permutation with the
+// fewest computed cells, tiles(n[p2]) * tiles(n[p1]) * n[p0] on tiles of 29
+// outputs per axis (depth 3); ties keep the view order.  Orders whose stored
+// plane has 2^31 cells or more are skipped (the fixed kernel's limit).
+std::array<int, 3> choose_order(const uint64_t n[3]) {
+  static const int ps[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  auto tiles = [](uint64_t m) { return (m + 28) / 29; };
+  std::array<int, 3> best = {0, 1, 2};
+  uint64_t best_cost = UINT64_MAX;
+  for (const auto& p : ps) {
+    if (n[p[1]] * n[p[2]] >= (1ull << 31)) continue;
+    const uint64_t cost = tiles(n[p[2]]) * tiles(n[p[1]]) * n[p[0]];
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = {p[0], p[1], p[2]};
+    }
+  }
+  return best;
+}
+
 template <int K, int R, int W>
 int launch_batch_kernel(int grid, const InstDev* insts, const int* item_inst, int ipb,
                         int nblocks, int steps, int64_t* a0, int64_t* a1, ScaleSlot* slots,
@@ -273,7 +341,12 @@ using namespace fdb::bt;
 
 struct fdb_batch {
   int count = 0;
-  std::vector<Geom> geoms;
+  std::vector<Geom> geoms;      // as stored (the kernels' geometry)
+  std::vector<Geom> geoms_ref;  // as described by the caller
+  std::vector<std::array<int, 3>> order;  // stored axis k = view axis order[k]
+  std::vector<char> permuted;
+  double* d_stage = nullptr;  // one instance in the caller's order
+  uint64_t stage_cells = 0;
   std::vector<int64_t> offsets;  // cells
   std::vector<uint64_t> sizes;
   int64_t total = 0;
@@ -499,9 +572,12 @@ int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
     const Coeffs3 c = coeffs3(g, dt[i]);
     double* bufs[2] = {b->arena[0] + b->offsets[i], b->arena[1] + b->offsets[i]};
     int cur = b->cur;
+    // depth and arithmetic as fdb_upwind_advect picks them for the described
+    // instance (the stored order does not change the fixed-point result)
+    const Geom& gr = b->geoms_ref[i];
     FixedTuning t;
-    t.depth = K > 0 ? K : 0;
-    if (fixed_supported(g, c, t.depth) == FDB_OK && (K > 0 || fixed_preferred(g))) {
+    t.depth = K > 0 ? K : default_depth(gr);
+    if (fixed_supported(g, c, t.depth) == FDB_OK && (K > 0 || fixed_preferred(gr))) {
       FDB_TRY(launch_advect_fixed_ex(g, c, steps, t, bufs, &cur, b->d_plain_scratch + i * per,
                                      per * 8, nullptr, b->stream));
     } else {
@@ -525,6 +601,20 @@ int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
 }
 
 int effective_K(fdb_batch* b) { return b->K > 0 ? b->K : 4; }
+
+// instance i between the caller's order and the stored order (see k_permute3)
+int launch_permute(fdb_batch* b, int i, const double* src, double* dst, bool to_view) {
+  uint64_t n3[3];
+  double v3[3], L3[3];
+  view3(b->geoms_ref[i], n3, v3, L3);
+  const std::array<int, 3>& o = b->order[i];
+  const uint64_t blocks = std::min<uint64_t>((b->sizes[i] + 255) / 256, 152 * 16);
+  k_permute3<<<(unsigned)blocks, 256, 0, b->stream>>>(src, dst, n3[0], n3[1], n3[2], o[0], o[1],
+                                                       o[2], to_view ? 1 : 0);
+  note_launch();
+  FDB_CUDA_TRY(cudaGetLastError());
+  return FDB_OK;
+}
 int effective_shape(fdb_batch* b) { return b->shape >= 0 ? b->shape : fx::kR4W8S; }
 
 }  // namespace
@@ -549,7 +639,34 @@ int fdb_batch_create(int count, const fdb_instance_desc* descs, fdb_batch** out)
       delete b;
       return rc;
     }
-    b->geoms.push_back(g);
+    // stored order: permuted only where the single-field path would run the
+    // (order-independent) fixed kernel
+    uint64_t n3[3];
+    double v3[3], L3[3];
+    view3(g, n3, v3, L3);
+    const std::array<int, 3> ord =
+        fixed_preferred(g) ? choose_order(n3) : std::array<int, 3>{0, 1, 2};
+    const bool perm = !(ord[0] == 0 && ord[1] == 1 && ord[2] == 2);
+    Geom gs = g;
+    if (perm) {
+      uint64_t np[3];
+      double vp[3], Lp[3];
+      for (int k = 0; k < 3; ++k) {
+        np[k] = n3[ord[k]];
+        vp[k] = v3[ord[k]];
+        Lp[k] = L3[ord[k]];
+      }
+      rc = make_geom(3, vp, Lp, np, &gs);
+      if (rc) {
+        delete b;
+        return rc;
+      }
+      b->stage_cells = std::max<uint64_t>(b->stage_cells, g.ntot);
+    }
+    b->geoms.push_back(gs);
+    b->geoms_ref.push_back(g);
+    b->order.push_back(ord);
+    b->permuted.push_back(perm ? 1 : 0);
     b->offsets.push_back(b->total);
     b->sizes.push_back(g.ntot);
     // keep every instance 256-byte aligned in the arenas
@@ -568,7 +685,8 @@ int fdb_batch_create(int count, const fdb_instance_desc* descs, fdb_batch** out)
       (rc = balloc(&b->d_done, count)) || (rc = balloc(&b->d_queue, 1)) ||
       (rc = balloc(&b->d_err, 1)) || (rc = balloc(&b->d_offs, count)) ||
       (rc = balloc(&b->d_sizes, count)) || (rc = balloc(&b->d_part, count * kSumPerInst)) ||
-      (rc = balloc(&b->d_sums, count)) || (rc = balloc(&b->d_plain_scratch, per * count))) {
+      (rc = balloc(&b->d_sums, count)) || (rc = balloc(&b->d_plain_scratch, per * count)) ||
+      (b->stage_cells && (rc = balloc(&b->d_stage, b->stage_cells)))) {
     fdb_batch_destroy(b);
     return rc;
   }
@@ -602,12 +720,19 @@ int fdb_batch_destroy(fdb_batch* b) {
   drop_graph(b);
   void* ps[] = {b->arena[0], b->arena[1], b->d_insts, b->d_item_inst, b->d_slots, b->d_done,
                 b->d_queue, b->d_err, b->d_offs, b->d_sizes, b->d_part, b->d_sums,
-                b->d_plain_scratch};
+                b->d_plain_scratch, b->d_stage};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (b->h_sums) cudaFreeHost(b->h_sums);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
+  return FDB_OK;
+}
+
+int fdb_batch_storage_order(fdb_batch* b, int index, int* order3) {
+  FDB_TRY(bcheck(b));
+  if (index < 0 || index >= b->count || !order3) return fail(FDB_ERR_INVALID, "bad index or output");
+  for (int k = 0; k < 3; ++k) order3[k] = b->order[index][k];
   return FDB_OK;
 }
 
@@ -625,16 +750,22 @@ int fdb_batch_count(fdb_batch* b, int* count, uint64_t* total_cells) {
 int fdb_batch_set_field(fdb_batch* b, int index, const double* src, int is_device) {
   FDB_TRY(bcheck(b));
   if (index < 0 || index >= b->count || !src) return fail(FDB_ERR_INVALID, "bad index or source");
-  FDB_CUDA_TRY(cudaMemcpyAsync(b->arena[b->cur] + b->offsets[index], src, b->sizes[index] * 8,
+  double* dst = b->arena[b->cur] + b->offsets[index];
+  const bool perm = b->permuted[index];
+  FDB_CUDA_TRY(cudaMemcpyAsync(perm ? b->d_stage : dst, src, b->sizes[index] * 8,
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                b->stream));
+  if (perm) FDB_TRY(launch_permute(b, index, b->d_stage, dst, false));
   return bsync(b);
 }
 
 int fdb_batch_get_field(fdb_batch* b, int index, double* dst, int is_device) {
   FDB_TRY(bcheck(b));
   if (index < 0 || index >= b->count || !dst) return fail(FDB_ERR_INVALID, "bad index or destination");
-  FDB_CUDA_TRY(cudaMemcpyAsync(dst, b->arena[b->cur] + b->offsets[index], b->sizes[index] * 8,
+  const double* src = b->arena[b->cur] + b->offsets[index];
+  const bool perm = b->permuted[index];
+  if (perm) FDB_TRY(launch_permute(b, index, src, b->d_stage, true));
+  FDB_CUDA_TRY(cudaMemcpyAsync(dst, perm ? b->d_stage : src, b->sizes[index] * 8,
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                b->stream));
   return bsync(b);
@@ -644,8 +775,13 @@ int fdb_batch_init_sphere(fdb_batch* b, int index, const double* center, double 
                           double noise_amp, uint64_t seed) {
   FDB_TRY(bcheck(b));
   if (index < 0 || index >= b->count || !center) return fail(FDB_ERR_INVALID, "bad index or centre");
-  FDB_TRY(launch_sphere_noise(b->geoms[index], center, radius, noise_amp, seed,
-                              b->arena[b->cur] + b->offsets[index], b->stream));
+  double* dst = b->arena[b->cur] + b->offsets[index];
+  const bool perm = b->permuted[index];
+  // generated in the caller's order (the generator is a function of the
+  // reference's cell index), then stored
+  FDB_TRY(launch_sphere_noise(b->geoms_ref[index], center, radius, noise_amp, seed,
+                              perm ? b->d_stage : dst, b->stream));
+  if (perm) FDB_TRY(launch_permute(b, index, b->d_stage, dst, false));
   return bsync(b);
 }
 

@@ -81,6 +81,8 @@ int launch_step_generic(const Geom& g, double dt, const double* in, double* out,
 // are outside what it serves (the caller then uses the FP64 kernel).
 int fixed_supported(const Geom& g, const Coeffs3& c, int depth);
 bool fixed_preferred(const Geom& g);
+// steps per launch the fixed kernel picks for g when none is asked for
+int default_depth(const Geom& g);
 size_t fixed_scratch_bytes();
 // Device error word inside the fixed kernel's scratch (non-zero: non-finite input).
 int* fixed_error_word(double* d_scratch);

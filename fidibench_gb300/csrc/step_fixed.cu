@@ -210,6 +210,8 @@ namespace {
 // x 32 computed cells per tile; the fastest measured shape at 160^3 - 512^3).
 constexpr int kDefaultShape = fx::kR4W8S;
 
+}  // namespace
+
 // Steps per launch for the default shape: the K that minimises the computed
 // tiles times the per-launch cost,
 //   ceil(nx / (32 - K)) * ceil(ny / (32 - K)) * (1 + 0.5 / K),
@@ -231,8 +233,6 @@ int default_depth(const Geom& g) {
   }
   return best;
 }
-
-}  // namespace
 
 int fixed_supported(const Geom& g, const Coeffs3& c, int depth) {
   if (g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "fixed kernel serves ndims <= 3");

@@ -182,6 +182,11 @@ typedef struct fdb_batch fdb_batch;
 int fdb_batch_create(int count, const fdb_instance_desc* descs, fdb_batch** out);
 int fdb_batch_destroy(fdb_batch* b);
 int fdb_batch_count(fdb_batch* b, int* count, uint64_t* total_cells);
+/* Stored axis order of instance `index`: stored axis k (z, y, x) is axis
+ * order3[k] of the instance's 3-D view (missing leading axes count as extent
+ * 1).  The batch picks the order with the fewest computed cells; fields go in
+ * and out in the caller's order regardless. */
+int fdb_batch_storage_order(fdb_batch* b, int index, int* order3);
 int fdb_batch_set_field(fdb_batch* b, int index, const double* src, int is_device);
 int fdb_batch_get_field(fdb_batch* b, int index, double* dst, int is_device);
 int fdb_batch_init_sphere(fdb_batch* b, int index, const double* center, double radius,
