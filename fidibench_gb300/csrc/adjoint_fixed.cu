@@ -130,11 +130,16 @@ struct AdjTileSmem {
   static constexpr int bytes() { return kNL * kLPlane * 8 + (DOTS ? kNF * kFPlane * 4 : 0); }
 };
 
+// The tile step of one field: CTA number bid of its grid (tiles x fastest,
+// then y, then z-slabs), the scale ring slots of this launch (the lead CTA
+// advances the ring and logs the output scale), sf the scale of the state in
+// fstate, and dslot this CTA's three partial sums (DOTS).
 template <int R, int W, bool DOTS>
-__global__ void __launch_bounds__(32 * W, kAMinBlocks)
-k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
-               int32_t* __restrict__ out_hi, const int32_t* __restrict__ fstate,
-               const int* __restrict__ fscale, const FixedArgs a, double* __restrict__ dpart) {
+__device__ __forceinline__ void adjoint_tile(
+    const int64_t* __restrict__ in, int64_t* __restrict__ out, int32_t* __restrict__ out_hi,
+    const int32_t* __restrict__ fstate, int sf, const FixedArgs& a, int bid,
+    const ScaleSlot* slot_in, ScaleSlot* slot_out, ScaleSlot* slot_reset, int* scale_log,
+    int* err, bool lead, double* __restrict__ dslot) {
   using SM = AdjTileSmem<R, W, DOTS>;
   static_assert(SM::kRows == 32, "the halo column is loaded by one warp");
   extern __shared__ __align__(16) int64_t s_dyn[];
@@ -147,22 +152,23 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  int bid = blockIdx.x;
   const int tile_x = bid % a.tiles_x;
   bid /= a.tiles_x;
   const int tile_y = bid % a.tiles_y;
   const int tile_z = bid / a.tiles_y;
 
+  // coefficients held in registers (a may live in global memory, which the
+  // stores below could alias as far as the compiler knows)
+  const QCoeff qz = a.qz, qy = a.qy, qx = a.qx;
   int s, d;
-  if (!fx::scale_from_slot(a.slot_in, a.guard, &s, &d) && tid == 0) atomicOr(a.err, 1);
-  if (blockIdx.x == 0 && tid == 0) {
-    a.slot_reset->m = 0ull;
-    a.slot_reset->kind = 1;
-    a.slot_out->s = s;
-    a.slot_out->kind = 1;
-    if (a.scale_log) *a.scale_log = s;
+  if (!fx::scale_from_slot(slot_in, a.guard, &s, &d) && tid == 0) atomicOr(err, 1);
+  if (lead && tid == 0) {
+    slot_reset->m = 0ull;
+    slot_reset->kind = 1;
+    slot_out->s = s;
+    slot_out->kind = 1;
+    if (scale_log) *scale_log = s;
   }
-  const int sf = DOTS ? *fscale : 0;
 
   // logical -> physical column and row offsets (periodic wrap, axis flips)
   const int gx = tile_x * 32 + lane;
@@ -256,7 +262,7 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
       const int64_t Dz = lm[r * SM::kLRow] - c;
       const int64_t Dy = l[r * SM::kLRow - SM::kLRow] - c;
       const int64_t Dx = l[r * SM::kLRow - 1] - c;
-      const int64_t nv = fixed_update_d(c, Dz, Dy, Dx, a.qz, a.qy, a.qx);
+      const int64_t nv = fixed_update_d(c, Dz, Dy, Dx, qz, qy, qx);
       if (kFull || (row_mask & (1u << r))) {
         if (DOTS) {
           const int32_t G = myf[fb * SM::kFPlane + r * 32];
@@ -347,7 +353,7 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
       }
     }
   }
-  fx::cta_or<W>(my_or, s_or, &a.slot_out->m);  // contains __syncthreads
+  fx::cta_or<W>(my_or, s_or, &slot_out->m);  // contains __syncthreads
   if (DOTS && tid < 3) {
     Acc128 t;
     for (int w = 0; w < W; ++w) {
@@ -356,8 +362,49 @@ k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
       u.hi = s_red_hi[tid][w];
       t.add(u);
     }
-    dpart[3 * blockIdx.x + tid] += t.to_double() * pow2(32 + kGShift - s - sf);
+    dslot[tid] += t.to_double() * pow2(32 + kGShift - s - sf);
   }
+}
+
+// One field: the ring slots come with the launch arguments.
+template <int R, int W, bool DOTS>
+__global__ void __launch_bounds__(32 * W, kAMinBlocks)
+k_adjoint_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out,
+               int32_t* __restrict__ out_hi, const int32_t* __restrict__ fstate,
+               const int* __restrict__ fscale, const FixedArgs a, double* __restrict__ dpart) {
+  adjoint_tile<R, W, DOTS>(in, out, out_hi, fstate, DOTS ? *fscale : 0, a, blockIdx.x, a.slot_in,
+                           a.slot_out, a.slot_reset, a.scale_log, a.err, blockIdx.x == 0,
+                           DOTS ? dpart + 3 * blockIdx.x : nullptr);
+}
+
+// Many fields in one launch (the batched adjoint): CTA b works on instance
+// cta_inst[b], whose CTAs start at insts[i].cta_base; every instance has its
+// own scale ring (position ring_pos of this launch), its own scale log and
+// its own place in the buffers.  All instances take the same step.
+struct AdjInst {
+  FixedArgs a;       // geometry, tiling, coefficients, guard (slot fields unused)
+  int64_t offset;    // first cell in the buffers
+  ScaleSlot* ring;   // 3 slots
+  int* logs;         // scale of each state of the segment
+  int cta_base;
+};
+
+template <int R, int W, bool DOTS>
+__global__ void __launch_bounds__(32 * W, kAMinBlocks)
+k_adjoint_tile_multi(const AdjInst* __restrict__ insts, const int* __restrict__ cta_inst,
+                     const int64_t* __restrict__ in, int64_t* __restrict__ out,
+                     int32_t* __restrict__ out_hi, const int32_t* __restrict__ fstate,
+                     int ring_pos, int log_out, int log_f, int* err,
+                     double* __restrict__ dpart) {
+  const AdjInst& I = insts[cta_inst[blockIdx.x]];
+  const int bid = blockIdx.x - I.cta_base;
+  ScaleSlot* r = I.ring;
+  adjoint_tile<R, W, DOTS>(in + I.offset, out + I.offset,
+                           DOTS ? nullptr : out_hi + I.offset,
+                           DOTS ? fstate + I.offset : nullptr, DOTS ? I.logs[log_f] : 0, I.a,
+                           bid, r + ring_pos % 3, r + (ring_pos + 1) % 3, r + (ring_pos + 2) % 3,
+                           log_out >= 0 ? I.logs + log_out : nullptr, err, bid == 0,
+                           DOTS ? dpart + 3 * blockIdx.x : nullptr);
 }
 
 // f (FP64) -> F (int64) with the scale of a kind-0 slot (max|f| pre-pass);
@@ -448,6 +495,116 @@ unsigned grid_for(uint64_t n) {
   uint64_t b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
   return (unsigned)std::max<uint64_t>(b, 1);
+}
+
+// ---- per-instance elementwise kernels of the batched adjoint ---------------
+// Block b works on part (b % per_inst) of instance b / per_inst; instance i
+// has cells [offs[i], offs[i] + sizes[i]) and the scale ring rings[3i..3i+2].
+constexpr int kPerInst = 16;
+
+__global__ void k_ring_init_multi(ScaleSlot* rings, int count) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * count; k += gridDim.x * blockDim.x) {
+    rings[k].m = 0ull;
+    rings[k].s = 0;
+    rings[k].kind = (k % 3 == 0) ? 0 : 1;
+  }
+}
+
+// max|f| bit patterns of each instance into slot 0 of its ring (kind 0)
+__global__ void __launch_bounds__(256)
+k_absmax_multi(const double* __restrict__ f, const int64_t* __restrict__ offs,
+               const uint64_t* __restrict__ sizes, ScaleSlot* rings) {
+  __shared__ unsigned long long sh[8];
+  const int i = blockIdx.x / kPerInst;
+  const int part = blockIdx.x - i * kPerInst;
+  const double* fi = f + offs[i];
+  const uint64_t n = sizes[i];
+  unsigned long long m = 0ull;
+  for (uint64_t k = (uint64_t)part * 256 + threadIdx.x; k < n; k += (uint64_t)kPerInst * 256) {
+    const unsigned long long b =
+        (unsigned long long)__double_as_longlong(__ldg(fi + k)) & 0x7FFFFFFFFFFFFFFFull;
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = v > m ? v : m;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) m = sh[w] > m ? sh[w] : m;
+    atomicMax(&rings[3 * i].m, m);
+  }
+}
+
+// f (FP64) -> F (int64) per instance, ring position 0 (slot 0 kind 0 in,
+// slot 1 out, slot 2 cleared); F_hi (nullable) receives F in 2^29 units and
+// logs (nullable) the scale, at logs[i * log_stride].
+__global__ void __launch_bounds__(256)
+k_to_fixed_multi(const double* __restrict__ f, int64_t* __restrict__ F,
+                 int32_t* __restrict__ F_hi, const int64_t* __restrict__ offs,
+                 const uint64_t* __restrict__ sizes, ScaleSlot* rings,
+                 const int* __restrict__ guards, int* logs, int log_stride, int* err) {
+  __shared__ unsigned long long s_or[8];
+  const int i = blockIdx.x / kPerInst;
+  const int part = blockIdx.x - i * kPerInst;
+  ScaleSlot* r = rings + 3 * i;
+  int s, d;
+  if (!fx::scale_from_slot(r, guards[i], &s, &d) && threadIdx.x == 0) atomicOr(err, 1);
+  if (part == 0 && threadIdx.x == 0) {
+    r[2].m = 0ull;
+    r[2].kind = 1;
+    r[1].s = s;
+    r[1].kind = 1;
+    if (logs) logs[i * log_stride] = s;
+  }
+  const int64_t o = offs[i];
+  const uint64_t n = sizes[i];
+  unsigned long long my_or = 0ull;
+  for (uint64_t k = (uint64_t)part * 256 + threadIdx.x; k < n; k += (uint64_t)kPerInst * 256) {
+    const int64_t v = to_fixed(__ldg(f + o + k), s);
+    F[o + k] = v;
+    if (F_hi) F_hi[o + k] = state_g(v);
+    my_or |= (unsigned long long)(v ^ (v >> 63));
+  }
+  fx::cta_or<8>(my_or, s_or, &r[1].m);
+}
+
+// F (int64, scale from ring slot ring_pos % 3) -> f (FP64) per instance
+__global__ void __launch_bounds__(256)
+k_to_double_multi(const int64_t* __restrict__ F, double* __restrict__ f,
+                  const int64_t* __restrict__ offs, const uint64_t* __restrict__ sizes,
+                  const ScaleSlot* rings, int ring_pos) {
+  const int i = blockIdx.x / kPerInst;
+  const int part = blockIdx.x - i * kPerInst;
+  const int s = __ldcg(&rings[3 * i + ring_pos % 3].s);
+  const int64_t o = offs[i];
+  const uint64_t n = sizes[i];
+  for (uint64_t k = (uint64_t)part * 256 + threadIdx.x; k < n; k += (uint64_t)kPerInst * 256)
+    f[o + k] = to_double(__ldg(F + o + k), s);
+}
+
+// per-instance sums of the CTA partials: block i adds CTAs
+// [cta_base[i], cta_base[i+1]) in a fixed order
+__global__ void __launch_bounds__(256)
+k_sum3_multi(const double* __restrict__ dpart, const int* __restrict__ cta_base,
+             double* __restrict__ out3) {
+  __shared__ double sh[256];
+  const int i = blockIdx.x;
+  const int b0 = cta_base[i], b1 = cta_base[i + 1];
+  for (int j = 0; j < 3; ++j) {
+    double acc = 0.0;
+    for (int b = b0 + threadIdx.x; b < b1; b += 256) acc += dpart[3 * b + j];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out3[3 * i + j] = sh[0];
+    __syncthreads();
+  }
 }
 
 }  // namespace
@@ -602,6 +759,181 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   }
   k_to_double<<<grid_for(n), 256, 0, st>>>(io.lam[lc], io.grad_f0, n, lr + (li % 3));
   k_sum3<<<1, 256, 0, st>>>(io.dpart, nblk, io.dda3);
+  note_launch(2);
+  FDB_CUDA_TRY(cudaGetLastError());
+  return FDB_OK;
+}
+
+// ---- batched adjoint ----------------------------------------------------
+
+// z-slab height of the batched launches: one common height such that the
+// launch is about two waves of resident CTAs (uneven instances then
+// balance), at least 4 planes.
+static int batch_slab_height(int count, const Geom* geoms) {
+  int64_t tile_planes = 0;
+  for (int i = 0; i < count; ++i)
+    tile_planes += ((geoms[i].nx + 31) / 32) * ((geoms[i].ny + 31) / 32) * geoms[i].nz;
+  const int64_t res = step1_resident();
+  return (int)std::max<int64_t>(4, (tile_planes + 2 * res - 1) / (2 * res));
+}
+
+static int batch_ctas_of(const Geom& g, int H) {
+  const int tz = (int)std::min<int64_t>(H, g.nz);
+  return (int)(((g.nx + 31) / 32) * ((g.ny + 31) / 32) * ((g.nz + tz - 1) / tz));
+}
+
+int batch_adjoint_grid(int count, const Geom* geoms) {
+  const int H = batch_slab_height(count, geoms);
+  int grid = 0;
+  for (int i = 0; i < count; ++i) grid += batch_ctas_of(geoms[i], H);
+  return grid;
+}
+
+namespace {
+struct BatchScratch {
+  AdjInst* insT;
+  AdjInst* insF;
+  int* cta_inst;
+  int* cta_base;
+  double* dpart;
+  ScaleSlot* ringsF;
+  ScaleSlot* ringsT;
+  int* logs;
+  int* guards;
+  size_t bytes;
+};
+BatchScratch carve(void* base, int count, int K, int grid) {
+  BatchScratch sc;
+  char* p = (char*)base;
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    char* q = p ? p + off : nullptr;
+    off += (n + 255) / 256 * 256;
+    return q;
+  };
+  sc.insT = (AdjInst*)take(sizeof(AdjInst) * count);
+  sc.insF = (AdjInst*)take(sizeof(AdjInst) * count);
+  sc.cta_inst = (int*)take(sizeof(int) * grid);
+  sc.cta_base = (int*)take(sizeof(int) * (count + 1));
+  sc.dpart = (double*)take(sizeof(double) * 3 * grid);
+  sc.ringsF = (ScaleSlot*)take(sizeof(ScaleSlot) * 3 * count);
+  sc.ringsT = (ScaleSlot*)take(sizeof(ScaleSlot) * 3 * count);
+  sc.logs = (int*)take(sizeof(int) * K * count);
+  sc.guards = (int*)take(sizeof(int) * count);
+  sc.bytes = off;
+  return sc;
+}
+}  // namespace
+
+size_t batch_adjoint_scratch_bytes(int count, int K, int grid) {
+  return carve(nullptr, count, K, grid).bytes;
+}
+
+static int set_multi_smem_limits() {
+  FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile_multi<kAR, kAW, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    AdjTileSmem<kAR, kAW, true>::bytes()));
+  FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile_multi<kAR, kAW, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    AdjTileSmem<kAR, kAW, false>::bytes()));
+  return FDB_OK;
+}
+
+int batch_adjoint_run(const BatchAdjointIO& io, cudaStream_t st) {
+  FDB_TRY(set_multi_smem_limits());
+  const int count = io.count;
+  const int H = batch_slab_height(count, io.geoms);
+  const int grid = batch_adjoint_grid(count, io.geoms);
+  const BatchScratch sc = carve(io.scratch, count, io.K, grid);
+  // per-instance tables: tiling and coefficients of the transposed and the
+  // forward step, ring, scale log and first CTA
+  std::vector<AdjInst> hT(count), hF(count);
+  std::vector<int> cta_inst, cta_base(count + 1), guards(count);
+  cta_inst.reserve(grid);
+  int next = 0;
+  for (int i = 0; i < count; ++i) {
+    const Geom& g = io.geoms[i];
+    const Coeffs3& c = io.coeffs[i];
+    for (int t = 0; t < 2; ++t) {
+      FixedArgs a = make_fixed_args(t == 0 ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
+                                    (int64_t)2 * 152);
+      a.tx = 32;
+      a.ty = kAR * kAW;
+      a.tiles_x = (a.nx + a.tx - 1) / a.tx;
+      a.tiles_y = (a.ny + a.ty - 1) / a.ty;
+      a.tz = std::min(H, a.nz);
+      a.tiles_z = (a.nz + a.tz - 1) / a.tz;
+      a.guard = guard_bits(c, 1);
+      a.scale_log = nullptr;
+      AdjInst& I = t == 0 ? hT[i] : hF[i];
+      I.a = a;
+      I.offset = io.offsets[i];
+      I.ring = (t == 0 ? sc.ringsT : sc.ringsF) + 3 * i;
+      I.logs = sc.logs + (size_t)i * io.K;
+      I.cta_base = next;
+    }
+    const int n = batch_ctas_of(g, H);
+    cta_base[i] = next;
+    for (int k = 0; k < n; ++k) cta_inst.push_back(i);
+    next += n;
+    guards[i] = guard_bits(c, 1);
+  }
+  cta_base[count] = next;
+  if (next != grid) return fail(FDB_ERR_INVALID, "batched adjoint tiling mismatch");
+  FDB_CUDA_TRY(cudaMemcpyAsync(sc.insT, hT.data(), sizeof(AdjInst) * count,
+                               cudaMemcpyHostToDevice, st));
+  FDB_CUDA_TRY(cudaMemcpyAsync(sc.insF, hF.data(), sizeof(AdjInst) * count,
+                               cudaMemcpyHostToDevice, st));
+  FDB_CUDA_TRY(cudaMemcpyAsync(sc.cta_inst, cta_inst.data(), sizeof(int) * grid,
+                               cudaMemcpyHostToDevice, st));
+  FDB_CUDA_TRY(cudaMemcpyAsync(sc.cta_base, cta_base.data(), sizeof(int) * (count + 1),
+                               cudaMemcpyHostToDevice, st));
+  FDB_CUDA_TRY(cudaMemcpyAsync(sc.guards, guards.data(), sizeof(int) * count,
+                               cudaMemcpyHostToDevice, st));
+  FDB_CUDA_TRY(cudaMemsetAsync(sc.dpart, 0, sizeof(double) * 3 * grid, st));
+  const unsigned eg = (unsigned)(count * kPerInst);
+  const unsigned rg = (unsigned)((3 * count + 255) / 256);
+  constexpr int kSmT = AdjTileSmem<kAR, kAW, true>::bytes();
+  constexpr int kSmF = AdjTileSmem<kAR, kAW, false>::bytes();
+
+  // lam_T -> int64 (adjoint rings, position 0)
+  k_ring_init_multi<<<rg, 256, 0, st>>>(sc.ringsT, count);
+  k_absmax_multi<<<eg, 256, 0, st>>>(io.lam_T, io.d_offs, io.d_sizes, sc.ringsT);
+  k_to_fixed_multi<<<eg, 256, 0, st>>>(io.lam_T, io.lam[0], nullptr, io.d_offs, io.d_sizes,
+                                       sc.ringsT, sc.guards, nullptr, 0, io.err);
+  note_launch(3);
+  int li = 1;  // adjoint ring position of the next launch
+  int lc = 0;
+  for (int sgi = io.nseg - 1; sgi >= 0; --sgi) {
+    const int len = std::min(io.K, io.S - sgi * io.K);
+    // states of the segment: state k in chain[k & 1] (int64) and in
+    // state_hi[k] (2^29 units), forward rings at position k
+    k_ring_init_multi<<<rg, 256, 0, st>>>(sc.ringsF, count);
+    k_absmax_multi<<<eg, 256, 0, st>>>(io.ckpt[sgi], io.d_offs, io.d_sizes, sc.ringsF);
+    k_to_fixed_multi<<<eg, 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], io.d_offs,
+                                         io.d_sizes, sc.ringsF, sc.guards, sc.logs, io.K, io.err);
+    note_launch(3);
+    for (int k = 1; k < len; ++k) {
+      k_adjoint_tile_multi<kAR, kAW, false><<<grid, 32 * kAW, kSmF, st>>>(
+          sc.insF, sc.cta_inst, io.chain[(k - 1) & 1], io.chain[k & 1], io.state_hi[k], nullptr,
+          k, k, -1, io.err, nullptr);
+      note_launch();
+    }
+    FDB_CUDA_TRY(cudaGetLastError());
+    // adjoint steps sK+len-1 .. sK
+    for (int k = len - 1; k >= 0; --k) {
+      k_adjoint_tile_multi<kAR, kAW, true><<<grid, 32 * kAW, kSmT, st>>>(
+          sc.insT, sc.cta_inst, io.lam[lc], io.lam[lc ^ 1], nullptr, io.state_hi[k], li, -1, k,
+          io.err, sc.dpart);
+      note_launch();
+      lc ^= 1;
+      ++li;
+    }
+    FDB_CUDA_TRY(cudaGetLastError());
+  }
+  k_to_double_multi<<<eg, 256, 0, st>>>(io.lam[lc], io.grad_f0, io.d_offs, io.d_sizes, sc.ringsT,
+                                        li);
+  k_sum3_multi<<<count, 256, 0, st>>>(sc.dpart, sc.cta_base, io.dda3);
   note_launch(2);
   FDB_CUDA_TRY(cudaGetLastError());
   return FDB_OK;

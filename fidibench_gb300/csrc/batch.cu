@@ -347,6 +347,16 @@ struct fdb_batch {
   std::vector<char> permuted;
   double* d_stage = nullptr;  // one instance in the caller's order
   uint64_t stage_cells = 0;
+  // batched adjoint storage (grown on demand): checkpoints, segment buffers
+  // (two int64 chains, then int32 states two per buffer), adjoint ping-pong,
+  // lambda_T / dL/df0 in the stored layout, the caller-order copy, scratch
+  std::vector<double*> adj_ckpt, adj_seg;
+  double* adj_lam[2] = {nullptr, nullptr};
+  double* adj_io[2] = {nullptr, nullptr};
+  double* adj_user = nullptr;
+  double* adj_dda = nullptr;
+  void* adj_scratch = nullptr;
+  size_t adj_scratch_bytes = 0;
   std::vector<int64_t> offsets;  // cells
   std::vector<uint64_t> sizes;
   int64_t total = 0;
@@ -602,6 +612,28 @@ int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
 
 int effective_K(fdb_batch* b) { return b->K > 0 ? b->K : 4; }
 
+void free_batch_adjoint(fdb_batch* b) {
+  for (double* p : b->adj_ckpt) cudaFree(p);
+  for (double* p : b->adj_seg) cudaFree(p);
+  b->adj_ckpt.clear();
+  b->adj_seg.clear();
+  for (double*& p : b->adj_lam) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  for (double*& p : b->adj_io) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  if (b->adj_user) cudaFree(b->adj_user);
+  if (b->adj_dda) cudaFree(b->adj_dda);
+  if (b->adj_scratch) cudaFree(b->adj_scratch);
+  b->adj_user = nullptr;
+  b->adj_dda = nullptr;
+  b->adj_scratch = nullptr;
+  b->adj_scratch_bytes = 0;
+}
+
 // instance i between the caller's order and the stored order (see k_permute3)
 int launch_permute(fdb_batch* b, int i, const double* src, double* dst, bool to_view) {
   uint64_t n3[3];
@@ -723,6 +755,7 @@ int fdb_batch_destroy(fdb_batch* b) {
                 b->d_plain_scratch, b->d_stage};
   for (void* p : ps)
     if (p) cudaFree(p);
+  free_batch_adjoint(b);
   if (b->h_sums) cudaFreeHost(b->h_sums);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
@@ -831,6 +864,142 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
   FDB_TRY(check_dts(b, dt));
   if (num_steps == 0) return FDB_OK;
   return run_looped(b, num_steps, dt, b->K);
+}
+
+int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
+                      double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
+  FDB_TRY(bcheck(b));
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  FDB_TRY(check_dts(b, dt));
+  if (!lambda_T || !grad_f0) return fail(FDB_ERR_INVALID, "null lambda_T or grad_f0");
+  if (checkpoint_every < 0) return fail(FDB_ERR_INVALID, "checkpoint_every must be >= 0");
+  const int S = num_steps;
+  int K = checkpoint_every;
+  if (K == 0) K = std::max(1, (int)ceil(sqrt((double)std::max(S, 1))));
+  if (K > std::max(S, 1)) K = std::max(S, 1);
+  const int nseg = (S + K - 1) / K;
+  const int n = b->count;
+  // every instance in the fixed kernel's domain (forward and transposed steps)
+  std::vector<Coeffs3> cs(n);
+  for (int i = 0; i < n; ++i) {
+    cs[i] = coeffs3(b->geoms[i], dt[i]);
+    if (fixed_supported(b->geoms[i], cs[i], 1) != FDB_OK ||
+        fixed_supported(b->geoms[i], cs[i], effective_K(b)) != FDB_OK)
+      return fail(FDB_ERR_UNSUPPORTED, "batched adjoint: instance " + std::to_string(i) +
+                                           " is outside the fixed-point kernel's domain");
+  }
+  // storage
+  const size_t T = (size_t)b->total;
+  const int nsegbuf = adjoint_fixed_segment_buffers(K);
+  const int grid = batch_adjoint_grid(n, b->geoms.data());
+  const size_t sb = batch_adjoint_scratch_bytes(n, K, grid);
+  if ((int)b->adj_ckpt.size() < nseg || (int)b->adj_seg.size() < nsegbuf || !b->adj_lam[0] ||
+      b->adj_scratch_bytes < sb) {
+    free_batch_adjoint(b);
+    b->adj_ckpt.assign(nseg, nullptr);
+    b->adj_seg.assign(nsegbuf, nullptr);
+    int rc = FDB_OK;
+    for (auto& p : b->adj_ckpt)
+      if (!rc) rc = balloc(&p, T);
+    for (auto& p : b->adj_seg)
+      if (!rc) rc = balloc(&p, T);
+    for (auto& p : b->adj_lam)
+      if (!rc) rc = balloc(&p, T);
+    for (auto& p : b->adj_io)
+      if (!rc) rc = balloc(&p, T);
+    if (!rc) rc = balloc(&b->adj_user, T);
+    if (!rc) rc = balloc(&b->adj_dda, 3 * (size_t)n);
+    if (!rc) rc = balloc((char**)&b->adj_scratch, sb);
+    if (rc) {
+      free_batch_adjoint(b);
+      return rc;
+    }
+    b->adj_scratch_bytes = sb;
+  }
+  // the caller's concatenated fields: instance i starts at pref[i]
+  std::vector<uint64_t> pref(n);
+  uint64_t cells = 0;
+  for (int i = 0; i < n; ++i) {
+    pref[i] = cells;
+    cells += b->sizes[i];
+  }
+  // forward with checkpoints (the persistent launch): ckpt[s] = f^{sK}
+  for (int sg = 0; sg < nseg; ++sg) {
+    FDB_CUDA_TRY(cudaMemcpyAsync(b->adj_ckpt[sg], b->arena[b->cur], T * 8,
+                                 cudaMemcpyDeviceToDevice, b->stream));
+    const int len = std::min(K, S - sg * K);
+    FDB_TRY(run_batched(b, len, dt, effective_K(b), effective_shape(b), b->tz, true));
+  }
+  // lambda_T into the stored layout
+  const double* lt = lambda_T;
+  if (!is_device) {
+    FDB_CUDA_TRY(cudaMemcpyAsync(b->adj_user, lambda_T, cells * 8, cudaMemcpyHostToDevice,
+                                 b->stream));
+    lt = b->adj_user;
+  }
+  for (int i = 0; i < n; ++i) {
+    double* dst = b->adj_io[0] + b->offsets[i];
+    if (b->permuted[i])
+      FDB_TRY(launch_permute(b, i, lt + pref[i], dst, false));
+    else
+      FDB_CUDA_TRY(cudaMemcpyAsync(dst, lt + pref[i], b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
+                                   b->stream));
+  }
+  BatchAdjointIO io;
+  std::vector<int32_t*> hi(K);
+  for (int k = 0; k < K; ++k) hi[k] = (int32_t*)b->adj_seg[2 + k / 2] + (k & 1) * T;
+  io.count = n;
+  io.geoms = b->geoms.data();
+  io.coeffs = cs.data();
+  io.offsets = b->offsets.data();
+  io.d_offs = b->d_offs;
+  io.d_sizes = b->d_sizes;
+  io.S = S;
+  io.K = K;
+  io.nseg = nseg;
+  io.ckpt = b->adj_ckpt.data();
+  io.chain[0] = (int64_t*)b->adj_seg[0];
+  io.chain[1] = (int64_t*)b->adj_seg[1];
+  io.state_hi = hi.data();
+  io.lam[0] = (int64_t*)b->adj_lam[0];
+  io.lam[1] = (int64_t*)b->adj_lam[1];
+  io.lam_T = b->adj_io[0];
+  io.grad_f0 = b->adj_io[1];
+  io.dda3 = b->adj_dda;
+  io.err = b->d_err;
+  io.scratch = b->adj_scratch;
+  FDB_TRY(batch_adjoint_run(io, b->stream));
+  // dL/df0 back to the caller's order
+  double* gd = is_device ? grad_f0 : b->adj_user;
+  for (int i = 0; i < n; ++i) {
+    const double* src = b->adj_io[1] + b->offsets[i];
+    if (b->permuted[i])
+      FDB_TRY(launch_permute(b, i, src, gd + pref[i], true));
+    else
+      FDB_CUDA_TRY(cudaMemcpyAsync(gd + pref[i], src, b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
+                                   b->stream));
+  }
+  if (!is_device)
+    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, b->adj_user, cells * 8, cudaMemcpyDeviceToHost,
+                                 b->stream));
+  std::vector<double> dda(3 * (size_t)n);
+  FDB_CUDA_TRY(cudaMemcpyAsync(dda.data(), b->adj_dda, dda.size() * 8, cudaMemcpyDeviceToHost,
+                               b->stream));
+  FDB_TRY(bsync(b));
+  if (grad_v) {
+    // stored axis k is view axis order[k], i.e. reference axis jj[order[k]];
+    // a_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j (-dt up_j / dx_j)
+    for (int i = 0; i < n; ++i) {
+      const Geom& gr = b->geoms_ref[i];
+      const int jj[3] = {gr.jz, gr.jy, gr.jx};
+      for (int k = 0; k < 3; ++k) grad_v[3 * i + k] = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        const int j = jj[b->order[i][k]];
+        if (j >= 0) grad_v[3 * i + j] = dda[3 * i + k] * (-dt[i] * (double)gr.up[j] / gr.dx[j]);
+      }
+    }
+  }
+  return FDB_OK;
 }
 
 int fdb_batch_checksums(fdb_batch* b, double* out) {

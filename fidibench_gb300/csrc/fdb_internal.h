@@ -153,4 +153,29 @@ inline int adjoint_fixed_segment_buffers(int K) { return 2 + (K + 1) / 2; }
 int adjoint_fixed_ctas(const Geom& g, const Coeffs3& c);
 int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st);
 
+// The same for many instances stepping together (adjoint_fixed.cu): every
+// launch covers all instances; buffers hold the instances at `offsets`.
+struct BatchAdjointIO {
+  int count;
+  const Geom* geoms;        // geometry of each instance as stored (host)
+  const Coeffs3* coeffs;    // host
+  const int64_t* offsets;   // host, cells
+  const int64_t* d_offs;    // device copies of offsets and sizes
+  const uint64_t* d_sizes;
+  int S, K, nseg;
+  double* const* ckpt;       // nseg FP64 buffers: the instances at step s K
+  int64_t* chain[2];         // recompute chain (int64)
+  int32_t* const* state_hi;  // K int32 buffers: the segment's states in 2^29 units
+  int64_t* lam[2];           // adjoint ping-pong (int64)
+  const double* lam_T;       // device, FP64
+  double* grad_f0;           // device, FP64
+  double* dda3;              // device [3 * count]: dL/da per stored axis (z, y, x)
+  int* err;                  // device error word (bit 0: non-finite input)
+  void* scratch;             // batch_adjoint_scratch_bytes(count, K, grid) bytes
+};
+// CTAs of one batched launch
+int batch_adjoint_grid(int count, const Geom* geoms);
+size_t batch_adjoint_scratch_bytes(int count, int K, int grid);
+int batch_adjoint_run(const BatchAdjointIO& io, cudaStream_t st);
+
 }  // namespace fdb

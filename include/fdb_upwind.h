@@ -196,6 +196,18 @@ int fdb_batch_set_stream(fdb_batch* b, void* cuda_stream);
 int fdb_batch_set_tuning(fdb_batch* b, int key, int value);
 int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt);
 int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt);
+/* Batched adjoint: fdb_upwind_adjoint for every instance at once (the
+ * fixed-point adjoint; FDB_ERR_UNSUPPORTED when an instance is outside the
+ * fixed kernel's domain).  The forward pass with checkpoints runs the
+ * persistent launch; every recompute and transposed step is one launch over
+ * all instances.  lambda_T and grad_f0 hold the instances' fields one after
+ * another in the caller's order (instance i starts at the sum of the sizes of
+ * instances 0..i-1); grad_v receives 3 values per instance (dL/dv per
+ * reference axis, 0 for missing axes; host memory); dt holds one time step
+ * per instance; checkpoint_every as in fdb_upwind_adjoint.  The batch's fields
+ * are left at f_T.  Field pointers are device memory when is_device = 1. */
+int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
+                      double* grad_f0, double* grad_v, int checkpoint_every, int is_device);
 /* checksum() of every instance (upwind.cxx:91-93) into out[count]; synchronises. */
 int fdb_batch_checksums(fdb_batch* b, double* out);
 /* Times the compiled (depth, shape, tile_z) choices on a copy of the fields
