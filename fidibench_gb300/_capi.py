@@ -59,6 +59,7 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_batch_count": (_int, [_vp, ctypes.POINTER(_int), _u64p]),
     "fdb_batch_storage_order": (_int, [_vp, _int, ctypes.POINTER(_int)]),
     "fdb_batch_adjoint": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _int, _int]),
+    "fdb_batch_set_velocity": (_int, [_vp, _int, _vp]),
     "fdb_batch_set_field": (_int, [_vp, _int, _vp, _int]),
     "fdb_batch_get_field": (_int, [_vp, _int, _vp, _int]),
     "fdb_batch_init_sphere": (_int, [_vp, _int, _vp, ctypes.c_double, ctypes.c_double,

@@ -9,7 +9,8 @@ ndims values.  Gradients flow to both: dL/df0 from the transposed steps and
 dL/dv from the per-step coefficient contractions (the upwind direction is
 piecewise constant in v, so dv is the derivative within the sign pattern).
 torch supplies only device memory and the autograd graph; every step runs in
-libfdb_upwind.
+libfdb_upwind.  batch_advect_fn does the same for many instances at once
+(fdb_batch_advect forward, fdb_batch_adjoint backward).
 """
 from __future__ import annotations
 
@@ -85,4 +86,91 @@ def advect_fn(f0, velocity, num_steps: int, dt: float, lengths=None, checkpoint_
     return UpwindAdvect.apply(f0, velocity, num_steps, dt, tuple(lengths), checkpoint_every)
 
 
-__all__ = ["UpwindAdvect", "advect_fn", "release_handles"]
+# ---- many instances at once (fdb_batch_advect / fdb_batch_adjoint) -------------
+
+_batches: dict = {}
+
+
+def _batch_handle(shapes, lengths, velocity, device):
+    from .batch import Batch
+    key = (tuple(shapes), tuple(lengths), str(device))
+    v = velocity.detach().to("cpu", torch.float64).numpy()
+    with _cache_lock:
+        entry = _batches.get(key)
+        if entry is None:
+            with torch.cuda.device(device):
+                b = Batch([(v[k, :len(n)], L, n) for k, (n, L) in enumerate(zip(shapes, lengths))])
+            entry = [b, v.copy()]
+            _batches[key] = entry
+    b, v_set = entry
+    for k, n in enumerate(shapes):
+        if not np.array_equal(v_set[k, :len(n)], v[k, :len(n)]):
+            b.set_velocity(k, v[k, :len(n)])
+            v_set[k, :len(n)] = v[k, :len(n)]
+    return b
+
+
+def release_batches() -> None:
+    """Free the cached batches (device memory)."""
+    with _cache_lock:
+        for b, _ in _batches.values():
+            b.close()
+        _batches.clear()
+
+
+class BatchAdvect(torch.autograd.Function):
+    """Many independent advections in one batch: f0 is one CUDA float64
+    tensor holding the instances' fields one after another (instance i starts
+    at the sum of the sizes of instances 0..i-1, each row-major), velocity a
+    (count, 3) float64 tensor (row i: the instance's velocity, zero-padded
+    beyond its axes), dts one time step per instance.  Forward: the batch's
+    persistent advect; backward: fdb_batch_adjoint, giving dL/df0 and dL/dv
+    for all instances at once."""
+
+    @staticmethod
+    def forward(ctx, f0, velocity, shapes, lengths, num_steps: int, dts,
+                checkpoint_every: int = 0):
+        if not f0.is_cuda or f0.dtype != torch.float64:
+            raise TypeError("f0 must be a CUDA float64 tensor")
+        b = _batch_handle(shapes, lengths, velocity, f0.device)
+        f0c = f0.detach().contiguous().view(-1)
+        b.set_fields(f0c)
+        b.advect(int(num_steps), dts)
+        out = torch.empty_like(f0c)
+        b.get_fields(out)
+        ctx.save_for_backward(f0c, velocity.detach())
+        ctx.meta = (tuple(shapes), tuple(lengths), int(num_steps), tuple(float(x) for x in dts),
+                    int(checkpoint_every))
+        return out.view_as(f0)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        f0c, velocity = ctx.saved_tensors
+        shapes, lengths, num_steps, dts, ck = ctx.meta
+        b = _batch_handle(shapes, lengths, velocity, f0c.device)
+        b.set_fields(f0c)
+        lam = grad_out.detach().to(torch.float64).contiguous().view(-1)
+        g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck)
+        grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device)
+        return g0.view_as(grad_out), grad_v, None, None, None, None, None
+
+
+def batch_advect_fn(f0, velocity, shapes, num_steps: int, dts, lengths=None,
+                    checkpoint_every: int = 0):
+    """Differentiable batched advect (see BatchAdvect): returns the
+    concatenated fields after num_steps steps."""
+    if lengths is None:
+        lengths = [(1.0,) * len(n) for n in shapes]
+    shapes = [tuple(int(x) for x in n) for n in shapes]
+    lengths = [tuple(float(x) for x in L) for L in lengths]
+    if not torch.is_tensor(velocity):
+        rows = np.zeros((len(shapes), 3))
+        for k, v in enumerate(velocity):
+            rows[k, :len(v)] = v
+        velocity = torch.tensor(rows, dtype=torch.float64)
+    return BatchAdvect.apply(f0, velocity, tuple(shapes), tuple(lengths), num_steps,
+                             tuple(float(x) for x in dts), checkpoint_every)
+
+
+__all__ = ["UpwindAdvect", "advect_fn", "release_handles", "BatchAdvect", "batch_advect_fn",
+           "release_batches"]

@@ -131,6 +131,51 @@ class Batch:
         check(lib.fdb_batch_get_field(self._h, int(index), out.ctypes.data, 0))
         return out
 
+    def set_fields(self, values) -> None:
+        """All fields from one concatenated array (instance i starts at
+        sum(sizes[:i])): numpy or a CUDA float64 tensor."""
+        total = sum(self.sizes)
+        dev = bool(getattr(values, "is_cuda", False))
+        if dev:
+            import torch
+            torch.cuda.current_stream(values.device).synchronize()  # torch's writes first
+            if values.numel() != total or not values.is_contiguous():
+                raise ValueError(f"need a contiguous tensor of {total} values")
+            base = values.data_ptr()
+        else:
+            values = np.ascontiguousarray(np.asarray(values, dtype=np.float64)).reshape(-1)
+            if values.size != total:
+                raise ValueError(f"need {total} values, got {values.size}")
+            base = values.ctypes.data
+        off = 0
+        for k, n in enumerate(self.sizes):
+            check(lib.fdb_batch_set_field(self._h, k, base + 8 * off, 1 if dev else 0))
+            off += n
+
+    def get_fields(self, out=None):
+        """All fields into one concatenated array (numpy, or `out`: a numpy
+        array or a contiguous CUDA float64 tensor)."""
+        total = sum(self.sizes)
+        if out is None:
+            out = np.empty(total, dtype=np.float64)
+        dev = bool(getattr(out, "is_cuda", False))
+        if dev and (out.numel() != total or not out.is_contiguous()):
+            raise ValueError(f"need a contiguous tensor of {total} values")
+        if not dev and out.size != total:
+            raise ValueError(f"need {total} values")
+        base = out.data_ptr() if dev else out.ctypes.data
+        off = 0
+        for k, n in enumerate(self.sizes):
+            check(lib.fdb_batch_get_field(self._h, k, base + 8 * off, 1 if dev else 0))
+            off += n
+        return out
+
+    def set_velocity(self, index: int, velocity) -> None:
+        v = np.ascontiguousarray(np.asarray(velocity, dtype=np.float64)).reshape(-1)
+        if v.size != len(self.shapes[index]):
+            raise ValueError("velocity needs one value per axis of the instance")
+        check(lib.fdb_batch_set_velocity(self._h, int(index), v.ctypes.data))
+
     def init_sphere(self, index: int, center, radius: float, noise_amp: float = 0.0,
                     seed: int = 0) -> None:
         c = np.ascontiguousarray(np.asarray(center, dtype=np.float64))

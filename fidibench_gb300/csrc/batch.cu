@@ -762,6 +762,35 @@ int fdb_batch_destroy(fdb_batch* b) {
   return FDB_OK;
 }
 
+int fdb_batch_set_velocity(fdb_batch* b, int index, const double* velocity) {
+  FDB_TRY(bcheck(b));
+  if (index < 0 || index >= b->count || !velocity)
+    return fail(FDB_ERR_INVALID, "bad index or velocity");
+  const Geom& old = b->geoms_ref[index];
+  Geom g;
+  FDB_TRY(make_geom(old.ndims, velocity, old.L, old.n, &g));
+  Geom gs = g;
+  if (b->permuted[index]) {
+    uint64_t n3[3];
+    double v3[3], L3[3];
+    view3(g, n3, v3, L3);
+    uint64_t np[3];
+    double vp[3], Lp[3];
+    const std::array<int, 3>& o = b->order[index];
+    for (int k = 0; k < 3; ++k) {
+      np[k] = n3[o[k]];
+      vp[k] = v3[o[k]];
+      Lp[k] = L3[o[k]];
+    }
+    FDB_TRY(make_geom(3, vp, Lp, np, &gs));
+  }
+  FDB_TRY(bsync(b));
+  b->geoms_ref[index] = g;
+  b->geoms[index] = gs;
+  drop_graph(b);
+  return FDB_OK;
+}
+
 int fdb_batch_storage_order(fdb_batch* b, int index, int* order3) {
   FDB_TRY(bcheck(b));
   if (index < 0 || index >= b->count || !order3) return fail(FDB_ERR_INVALID, "bad index or output");

@@ -192,6 +192,8 @@ int fdb_batch_get_field(fdb_batch* b, int index, double* dst, int is_device);
 int fdb_batch_init_sphere(fdb_batch* b, int index, const double* center, double radius,
                           double noise_amp, uint64_t seed);
 int fdb_batch_set_stream(fdb_batch* b, void* cuda_stream);
+/* New velocity of one instance (ndims values); the field is kept. */
+int fdb_batch_set_velocity(fdb_batch* b, int index, const double* velocity);
 /* keys FDB_TUNE_DEPTH, FDB_TUNE_SHAPE (2, 3 or 4), FDB_TUNE_TILE_Z */
 int fdb_batch_set_tuning(fdb_batch* b, int key, int value);
 int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt);
