@@ -132,3 +132,60 @@ def test_batch_adjoint_velocity_finite_differences(fdb):
             rp, rm = fp - target[k], fm - target[k]
             fd = float(np.sum((rp - rm) * (rp + rm))) / (4.0 * h)
             assert gv[k, j] == pytest.approx(fd, rel=1e-6), (k, j)
+
+
+@pytest.mark.parametrize("steps,ck", [(0, 0), (1, 0), (6, 1), (5, 9), (11, 4)])
+def test_batch_adjoint_step_and_checkpoint_counts(fdb, steps, ck):
+    specs = SPECS[1:4]
+    rng = np.random.default_rng(35)
+    dts = _dts(specs)
+    f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in specs]
+    lam = [rng.standard_normal(x.size) for x in f0]
+    b = _batch(fdb, specs, f0)
+    g0, gv = b.adjoint(steps, dts, np.concatenate(lam), checkpoint_every=ck)
+    off = np.cumsum([0] + [x.size for x in f0])
+    for k, s in enumerate(specs):
+        up = fdb.Upwind(s["v"], s["L"], s["n"])
+        up.f = f0[k]
+        g_ref, gv_ref = up.adjoint(steps, dts[k], lam[k], checkpoint_every=ck)
+        assert np.array_equal(g0[off[k]:off[k + 1]], g_ref), k
+        nd = len(s["n"])
+        assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-12,
+                           atol=1e-12 * max(np.abs(gv_ref).max(), 1e-300)), k
+        up.close()
+    b.close()
+
+
+def test_batch_adjoint_rejects_bad_input(fdb):
+    from fidibench_gb300._capi import FdbError
+    specs = SPECS[1:3]
+    b = _batch(fdb, specs, [np.ones(int(np.prod(s["n"]))) for s in specs])
+    total = sum(b.sizes)
+    with pytest.raises(ValueError):
+        b.adjoint(3, _dts(specs), np.zeros(total - 1))
+    # a Courant number above 1 is outside the fixed kernel's domain
+    bad = _dts(specs)
+    bad[1] *= 10.0
+    with pytest.raises(FdbError):
+        b.adjoint(3, bad, np.zeros(total))
+    b.close()
+
+
+def test_batch_set_velocity(fdb):
+    """After set_velocity the batch advects the new problem."""
+    specs = SPECS[:2]
+    rng = np.random.default_rng(36)
+    f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in specs]
+    b = _batch(fdb, specs, f0)
+    v_new = (-0.6, 0.35, 0.8)
+    b.set_velocity(0, v_new)
+    moved = [dict(specs[0], v=v_new), specs[1]]
+    dts = _dts(moved)
+    b.advect(8, dts)
+    for k, s in enumerate(moved):
+        up = fdb.Upwind(s["v"], s["L"], s["n"])
+        up.f = f0[k]
+        up.advect(8, dts[k])
+        assert rel_maxnorm(b.get_field(k), up.f) <= 1e-13, k
+        up.close()
+    b.close()
