@@ -17,13 +17,15 @@
 // across planes; each CTA adds its three sums into its own slot of a
 // per-call array (fixed CTA -> tile map, so the result is deterministic).
 //
-// Forward states f^n of a checkpoint segment are recomputed with one step
-// per launch by the same kernel without the transpose and the contraction:
-// the int64 chain goes through two ping-pong buffers and each state is also
-// stored in 2^29 units (int32, one array per step of the segment).
-// Each launch logs its output scale on the device, which the adjoint launch
-// for that step reads.  Elementwise kernels convert FP64 <-> int64 at the
-// ends.
+// Forward states f^n of a checkpoint segment are recomputed by the
+// temporally blocked forward kernel (step_fixed.cuh, several steps per
+// launch), which also stores every level of its output cells in 2^29 units
+// (int32, one array per step of the segment); the int64 chain goes through
+// two ping-pong buffers.  Each launch logs the scale of its levels on the
+// device, which the adjoint launch for that step reads.  The batched adjoint
+// recomputes with the tile kernel below without the transpose and the
+// contraction, one step per launch over all instances.  Elementwise kernels
+// convert FP64 <-> int64 at the ends.
 #include <math.h>
 
 #include <algorithm>
@@ -35,24 +37,15 @@
 namespace fdb {
 
 using fx::FixedArgs;
+using fx::kGShift;
 using fx::ScaleSlot;
+using fx::state_g;
 
 namespace {
 
 constexpr int kAR = 4;  // rows per thread
 constexpr int kAW = 8;  // warps per CTA
 constexpr int kAMinBlocks = 3;  // resident CTAs per SM the registers are sized for
-
-// The contraction reads a state F as G = floor(F / 2^kGShift): every
-// launch's output has |F| < 2^59 (scale_from_slot puts the input below
-// 2^(59 - guard); the guard bits cover the step's growth; one step's
-// rounding adds at most 8 units), so |G| <= 2^30 fits int32.  Flooring
-// rather than rounding shifts G by half a unit on average, and a constant
-// shift adds nothing: sum_i D_j[i] = 0 over the periodic grid.
-constexpr int kGShift = 29;
-__device__ __forceinline__ int32_t state_g(int64_t v) {
-  return (int32_t)(v >> kGShift);
-}
 
 // floor(a * b / 2^32) (one IMAD.HI)
 __device__ __forceinline__ int32_t mulhi_s(int32_t a, int32_t b) {
@@ -628,9 +621,6 @@ static int set_smem_limits() {
   FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile<kAR, kAW, true>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     AdjTileSmem<kAR, kAW, true>::bytes()));
-  FDB_CUDA_TRY(cudaFuncSetAttribute(k_adjoint_tile<kAR, kAW, false>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    AdjTileSmem<kAR, kAW, false>::bytes()));
   return FDB_OK;
 }
 
@@ -693,9 +683,9 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   const int gK = guard_bits(c, 1);
   FixedArgs aT = step1_args(g, c, true);
   aT.err = err;
-  FixedArgs aF = step1_args(g, c, false);
-  aF.err = err;
-  const int nblk = grid_of(aT), nblkF = grid_of(aF);
+  const int nblk = grid_of(aT);
+  // steps per recompute launch: the forward kernel's own choice for g
+  const int kRec = default_depth(g);
   if (nblk > io.dpart_cap) return fail(FDB_ERR_INVALID, "adjoint partial-sum buffer too small");
 
   // lam_T -> int64 (adjoint ring, launch index 0)
@@ -716,23 +706,24 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       cudaEventCreate(&e2);
       cudaEventRecord(e0, st);
     }
-    // states f^{sK} .. f^{sK+len-1} (forward ring, launch index 0..len-1):
-    // state k in int64 in chain[k & 1], in 2^29 units in state_hi[k]
+    // states f^{sK} .. f^{sK+len-1}: state 0 from the checkpoint (forward
+    // ring position 0), then the temporally blocked forward kernel, kRec
+    // steps per launch, which stores every level in state_g units; the int64
+    // chain ping-pongs between the two chain buffers
     k_ring_init<<<1, 32, 0, st>>>(fr);
     k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], n, fr);
     k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], n, fr,
                                            fr + 1, fr + 2, gK, logs + 0, err);
     note_launch(3);
-    for (int k = 1; k < len; ++k) {
-      aF.slot_in = fr + (k % 3);
-      aF.slot_out = fr + ((k + 1) % 3);
-      aF.slot_reset = fr + ((k + 2) % 3);
-      aF.scale_log = logs + k;
-      k_adjoint_tile<kAR, kAW, false>
-          <<<nblkF, 32 * kAW, AdjTileSmem<kAR, kAW, false>::bytes(), st>>>(
-              io.chain[(k - 1) & 1], io.chain[k & 1], io.state_hi[k], nullptr, nullptr, aF,
-              nullptr);
-      note_launch();
+    int cc = 0;   // chain buffer of the latest state
+    int pos = 1;  // forward ring position of the next launch
+    for (int k = 1; k < len;) {
+      const int kb = std::min(kRec, len - k);
+      FDB_TRY(launch_fixed_one(g, c, fx::kR4W8S, kb, io.chain[cc], io.chain[cc ^ 1], false, false,
+                               fr, pos, err, 0, kRec, logs + k, st, io.state_hi + k));
+      cc ^= 1;
+      ++pos;
+      k += kb;
     }
     FDB_CUDA_TRY(cudaGetLastError());
     if (io.recompute_ev) {

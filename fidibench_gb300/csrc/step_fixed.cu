@@ -173,7 +173,10 @@ long long plan_slabs(FixedArgs& a, int resident, int cap) {
 
 int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
                      bool in_f64, bool out_f64, ScaleSlot* slots, int i, int* err,
-                     int tz_override, int guard_K, int* scale_log, cudaStream_t st) {
+                     int tz_override, int guard_K, int* scale_log, cudaStream_t st,
+                     int32_t* const* gout) {
+  if (gout && (shape != fx::kR4W8S || in_f64 || out_f64 || K < 1 || K > 4))
+    return fail(FDB_ERR_UNSUPPORTED, "level output needs the default shape and int64 in/out");
   // 8 x 152 resident 256-thread CTAs, scaled to this shape's CTA size
   FixedArgs a = make_fixed_args(g, c, shape, K, tz_override,
                                 (int64_t)2 * 152 * 256 / (32 * fx::shape_warps(shape)));
@@ -192,6 +195,13 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
   const int64_t* pin = (const int64_t*)in;
   int64_t* pout = (int64_t*)out;
   const int cap = tz_override > 0 ? tz_override : 0;
+  if (gout) {
+    for (int t = 0; t < K; ++t) a.gout[t] = gout[t];
+    fx::launch_r4w8s_store_g(K, cap, pin, pout, a, st);
+    note_launch();
+    FDB_CUDA_TRY(cudaGetLastError());
+    return FDB_OK;
+  }
   switch (shape) {
     case fx::kR4W16: fx::launch_r4w16(K, in_f64, out_f64, cap, pin, pout, a, st); break;
     case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, cap, pin, pout, a, st); break;

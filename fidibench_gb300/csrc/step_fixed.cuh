@@ -34,7 +34,19 @@ struct FixedArgs {
   ScaleSlot* slot_reset;
   int* err;
   int* scale_log;  // nullable: block 0 records the scale of this launch's output
+  // STORE_G launches (the adjoint's recompute): level t+1 of every output
+  // cell, in state_g units, into gout[t]; scale_log[t] receives the scale
+  int32_t* gout[4];
 };
+
+// A state as the adjoint's contraction reads it: G = floor(F / 2^kGShift).
+// Every launch's output has |F| < 2^59 (scale_from_slot puts the input below
+// 2^(59 - guard); the guard bits cover the launch's growth; the roundings add
+// at most 8 units per step), so |G| <= 2^30 fits int32.  Flooring rather than
+// rounding shifts G by half a unit on average, and a constant shift adds
+// nothing to the contraction: sum_i D_j[i] = 0 over the periodic grid.
+constexpr int kGShift = 29;
+__device__ __forceinline__ int32_t state_g(int64_t v) { return (int32_t)(v >> kGShift); }
 
 __device__ __forceinline__ int wrap_mod(int i, int n) {
   int r = i % n;
@@ -111,7 +123,7 @@ enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1 };
 // logical axes (Z0 + nout <= nz); the CTA computes a (32) x (R*W) x (nout+K)
 // region that starts K cells upstream on every axis.  my_or accumulates |F| bits of the stored
 // outputs.  Callers synchronise the CTA before reusing shared memory.
-template <int K, int R, int W, bool HSM, int LOADER>
+template <int K, int R, int W, bool HSM, int LOADER, bool STORE_G = false>
 __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int Z0,
                                              int nout, int levels, bool in_f64, bool out_f64, int s, int d,
                                              const int64_t* __restrict__ in,
@@ -258,6 +270,12 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
       __syncthreads();
       row(0, (warp > 0) ? s_row[parity][warp - 1][lane] : cur[0]);
       parity ^= 1;
+      if (STORE_G && p >= K) {
+        int32_t* g = a.gout[t] + po;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (row_mask & (1u << r)) g[roff[r]] = state_g(cur[r]);
+      }
     }
     if (p >= K) {
       int64_t* dst = out + po;
@@ -303,7 +321,7 @@ __device__ __forceinline__ void cta_or(unsigned long long my_or, unsigned long l
 // their halo rows through L2, and the slabs shrink towards the end of the
 // grid so that the last wave is short (the scheduler hands out CTAs in
 // index order).
-template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64>
+template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64, bool STORE_G = false>
 __global__ void __launch_bounds__(32 * W, MINB)
 k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
   extern __shared__ __align__(16) int64_t s_dyn[];
@@ -323,11 +341,18 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
     a.slot_reset->kind = 1;
     a.slot_out->s = s;
     a.slot_out->kind = 1;
-    if (a.scale_log) *a.scale_log = s;
+    if (a.scale_log) {
+      // every level of the launch is held at scale s
+      if (STORE_G)
+        for (int t = 0; t < K; ++t) a.scale_log[t] = s;
+      else
+        *a.scale_log = s;
+    }
   }
   unsigned long long my_or = 0ull;
-  advance_tile<K, R, W, HSM, kLoadCpAsync>(a, tile % a.tiles_x, tile / a.tiles_x, z0, nout, K,
-                                           IN_F64, OUT_F64, s, d, in, out, s_dyn, s_row, my_or);
+  advance_tile<K, R, W, HSM, kLoadCpAsync, STORE_G>(a, tile % a.tiles_x, tile / a.tiles_x, z0,
+                                                    nout, K, IN_F64, OUT_F64, s, d, in, out,
+                                                    s_dyn, s_row, my_or);
   cta_or<W>(my_or, s_or, &a.slot_out->m);
 }
 
@@ -345,16 +370,17 @@ constexpr int shape_warps(int sh) {
 // resident CTA down to 8.  Sets a.nslab / a.slab_z; returns the CTA count.
 long long plan_slabs(FixedArgs& a, int resident, int cap);
 
-template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT>
+template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT, bool STORE_G = false>
 void launch_k(int cap, const int64_t* in, int64_t* out, FixedArgs a, cudaStream_t st) {
   constexpr int smem = fixed_smem_bytes<K, R, W, HSM>();
   static int per_sm = -1;  // per instantiation; benign race (idempotent)
   if (per_sm < 0) {
-    cudaFuncSetAttribute(k_advect_fixed<K, R, W, HSM, MINB, IN, OUT>,
+    cudaFuncSetAttribute(k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, k_advect_fixed<K, R, W, HSM, MINB, IN, OUT>, 32 * W, smem) != cudaSuccess)
+            &occ, k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>, 32 * W, smem) !=
+        cudaSuccess)
       occ = 1;
     per_sm = occ > 0 ? occ : 1;
   }
@@ -363,7 +389,20 @@ void launch_k(int cap, const int64_t* in, int64_t* out, FixedArgs a, cudaStream_
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long blocks = plan_slabs(a, per_sm * (sms > 0 ? sms : 1), cap);
   if (blocks <= 0) return;
-  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT><<<(unsigned)blocks, 32 * W, smem, st>>>(in, out, a);
+  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>
+      <<<(unsigned)blocks, 32 * W, smem, st>>>(in, out, a);
+}
+
+// int64 in and out, every level also stored in state_g units (a.gout)
+template <int R, int W, bool HSM, int MINB>
+void launch_shape_store_g(int K, int cap, const int64_t* in, int64_t* out, const FixedArgs& a,
+                          cudaStream_t st) {
+  switch (K) {
+    case 1: launch_k<1, R, W, HSM, MINB, false, false, true>(cap, in, out, a, st); break;
+    case 2: launch_k<2, R, W, HSM, MINB, false, false, true>(cap, in, out, a, st); break;
+    case 3: launch_k<3, R, W, HSM, MINB, false, false, true>(cap, in, out, a, st); break;
+    default: launch_k<4, R, W, HSM, MINB, false, false, true>(cap, in, out, a, st); break;
+  }
 }
 
 template <int K, int R, int W, bool HSM, int MINB>
@@ -393,9 +432,12 @@ fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K,
 int guard_bits(const Coeffs3& c, int K);
 // One launch of the single-field kernel (K steps, explicit buffers and slot
 // ring position i); scale_log (nullable, device) receives the output scale.
+// gout (nullable; K arrays, int64 in and out, default shape only): every level
+// of the launch stored in state_g units, its scale in scale_log[0..K).
 int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const void* in, void* out,
                      bool in_f64, bool out_f64, fx::ScaleSlot* slots, int i, int* err,
-                     int tz_override, int guard_K, int* scale_log, cudaStream_t st);
+                     int tz_override, int guard_K, int* scale_log, cudaStream_t st,
+                     int32_t* const* gout = nullptr);
 namespace fx {
 
 // defined in step_fixed_<shape>.cu; cap as in plan_slabs
@@ -403,6 +445,9 @@ namespace fx {
   void NAME(int K, bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,    \
             const FixedArgs& a, cudaStream_t st);
 FDB_FX_DECLARE(launch_r8w8)
+// the default shape with every level stored (the adjoint's recompute)
+void launch_r4w8s_store_g(int K, int cap, const int64_t* in, int64_t* out, const FixedArgs& a,
+                          cudaStream_t st);
 FDB_FX_DECLARE(launch_r4w16)
 FDB_FX_DECLARE(launch_r8w8s)
 FDB_FX_DECLARE(launch_r4w16s)

@@ -11,5 +11,10 @@ void launch_r4w8s(int K, bool in_f64, bool out_f64, int cap, const int64_t* in,
   launch_shape<4, 8, true, 2>(K, in_f64, out_f64, cap, in, out, a, st);
 }
 
+void launch_r4w8s_store_g(int K, int cap, const int64_t* in, int64_t* out, const FixedArgs& a,
+                          cudaStream_t st) {
+  launch_shape_store_g<4, 8, true, 2>(K, cap, in, out, a, st);
+}
+
 }  // namespace fx
 }  // namespace fdb

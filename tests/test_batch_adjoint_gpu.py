@@ -49,8 +49,11 @@ def test_batch_adjoint_matches_single_field(fdb):
         # the transposed steps are integer arithmetic: identical whatever the
         # tiling or the stored axis order
         assert np.array_equal(g0[off[k]:off[k + 1]], g_ref), k
+        # dL/dv: both contract with the forward states in 2^29 units, the
+        # batch's recomputed one step per launch, the handle's several steps
+        # per launch at one scale, so they agree to that precision
         nd = len(s["n"])
-        assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-12, atol=1e-12 * np.abs(gv_ref).max()), k
+        assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-8, atol=1e-8 * np.abs(gv_ref).max()), k
         assert np.all(gv[k, nd:] == 0.0)
         # the batch is left at f_T, as the single-field handle
         assert np.array_equal(b.get_field(k), up.f), k
@@ -150,8 +153,8 @@ def test_batch_adjoint_step_and_checkpoint_counts(fdb, steps, ck):
         g_ref, gv_ref = up.adjoint(steps, dts[k], lam[k], checkpoint_every=ck)
         assert np.array_equal(g0[off[k]:off[k + 1]], g_ref), k
         nd = len(s["n"])
-        assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-12,
-                           atol=1e-12 * max(np.abs(gv_ref).max(), 1e-300)), k
+        assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-8,
+                           atol=1e-8 * max(np.abs(gv_ref).max(), 1e-300)), k
         up.close()
     b.close()
 
