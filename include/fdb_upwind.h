@@ -36,7 +36,7 @@ extern "C" {
 #define FDB_ERR_INVALID 1      /* bad argument (sizes, dims, null pointers)    */
 #define FDB_ERR_CUDA 2         /* a CUDA runtime call or kernel launch failed  */
 #define FDB_ERR_ALLOC 3        /* device or pinned allocation failed           */
-#define FDB_ERR_UNSUPPORTED 4  /* valid request that this build does not serve */
+#define FDB_ERR_UNSUPPORTED 4  /* valid request that this library does not serve */
 #define FDB_ERR_TIMEOUT 5      /* a bounded device-side wait gave up           */
 #define FDB_ERR_NONFINITE 6    /* finiteness check found a NaN/Inf             */
 #define FDB_ERR_INJECTED 7     /* host-side fault injection (FDB_FAULT)        */
