@@ -9,11 +9,15 @@
 // positional "32 10" of the ctest cases) are ignored; an unknown -option prints
 // "<arg> is not a valid option." and the help text.  Added options:
 //   -arith <auto|exact|fma|fixed>  -courant <double> (0.1)  -json
+//   -velocity <vx,vy,vz> (1,1,1)  -adjoint (dL/dv of 0.5 sum f_T^2, and |dL/df0|)
 #include <chrono>
+#include <cmath>
 #include <cstdlib>
+#include <iomanip>
 #include <iostream>
 #include <limits>
 #include <map>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -45,6 +49,10 @@ int main(int argc, char** argv) {
   o.help["-arith"] = "Step arithmetic: auto, exact, fma or fixed";
   o.values["-courant"] = "0.1";
   o.help["-courant"] = "Courant number used to pick dt";
+  o.values["-velocity"] = "1,1,1";
+  o.help["-velocity"] = "Velocity components vx,vy,vz (the reference driver's is 1,1,1)";
+  o.flags["-adjoint"] = false;
+  o.help["-adjoint"] = "Also print dL/dv of L = 0.5 sum f_T^2 (the adjoint)";
   o.flags["-vtk"] = false;
   o.help["-vtk"] = "Write output to VTK file";
   o.flags["-std"] = false;
@@ -72,12 +80,19 @@ int main(int argc, char** argv) {
   std::cout << "number of time steps: " << numTimeSteps << '\n';
 
   std::vector<double> velocity(numCells.size(), 1.0);
+  {
+    std::stringstream vs(o.values["-velocity"]);
+    std::string item;
+    for (size_t j = 0; j < velocity.size() && std::getline(vs, item, ','); ++j)
+      velocity[j] = std::atof(item.c_str());
+  }
   std::vector<double> lengths(numCells.size(), 1.0);
   const double courant = std::atof(o.values["-courant"].c_str());
   double dt = std::numeric_limits<double>::max();
   for (size_t j = 0; j < velocity.size(); ++j) {
     const double dx = lengths[j] / numCells[j];
-    const double val = courant * dx / velocity[j];
+    if (velocity[j] == 0.0) continue;
+    const double val = courant * dx / std::fabs(velocity[j]);
     dt = (val < dt ? val : dt);
   }
 
@@ -85,6 +100,7 @@ int main(int argc, char** argv) {
     Upwind<ndims> up(velocity, lengths, numCells);
     up.setArith(arith_code(o.values["-arith"]));
     if (o.flags["-vtk"]) up.saveVTK("up0.vtk");
+    const std::vector<double> f0 = o.flags["-adjoint"] ? up.getField() : std::vector<double>();
     const auto t0 = std::chrono::steady_clock::now();
     up.advect(numTimeSteps, dt);
     const double cs = up.checksum();
@@ -92,6 +108,18 @@ int main(int argc, char** argv) {
     std::cout << "check sum: " << cs << '\n';
     if (o.flags["-std"]) std::cout << "std      : " << up.std() << '\n';
     if (o.flags["-vtk"]) up.saveVTK("up1.vtk");
+    if (o.flags["-adjoint"]) {
+      // L = 0.5 sum f_T^2: lambda_T = f_T, then from f0 again
+      const std::vector<double> lamT = up.getField();
+      up.setInitialCondition(f0);
+      std::vector<double> gv;
+      const std::vector<double> g0 = up.adjoint(numTimeSteps, dt, lamT, &gv);
+      double nrm = 0.0;
+      for (double x : g0) nrm += x * x;
+      std::cout << std::setprecision(17) << "dL/dv:";
+      for (double x : gv) std::cout << ' ' << x;
+      std::cout << "\n|dL/df0|: " << std::sqrt(nrm) << '\n' << std::setprecision(6);
+    }
     if (o.flags["-json"]) {
       const double cells = (double)n * n * n;
       std::cout << "{\"cells\": " << cells << ", \"steps\": " << numTimeSteps

@@ -113,6 +113,26 @@ class Upwind {
     return f;
   }
 
+  // Gradients of a loss L(f_T) given lambdaT = dL/df_T (no reference
+  // counterpart; fdb_upwind_adjoint): runs advect(numTimeSteps, deltaTime)
+  // from the current field with a checkpoint every checkpointEvery steps
+  // (0: about sqrt(numTimeSteps)), then the transposed steps.  Returns
+  // dL/df0; gradVelocity (nullable) receives dL/dv (NDIMS values).  The field
+  // ends at f_T, as after advect.
+  std::vector<double> adjoint(int numTimeSteps, double deltaTime,
+                              const std::vector<double>& lambdaT,
+                              std::vector<double>* gradVelocity = nullptr,
+                              int checkpointEvery = 0) {
+    if (lambdaT.size() != ntot_) throw std::invalid_argument("adjoint: wrong lambdaT size");
+    std::vector<double> g(ntot_);
+    std::vector<double> gv(NDIMS, 0.0);
+    check(fdb_upwind_adjoint(h_, numTimeSteps, deltaTime, lambdaT.data(), g.data(), gv.data(),
+                             checkpointEvery, 0),
+          "fdb_upwind_adjoint");
+    if (gradVelocity) *gradVelocity = gv;
+    return g;
+  }
+
   void setArith(int arith, int temporalDepth = 0) {
     check(fdb_upwind_set_arith(h_, arith, temporalDepth), "fdb_upwind_set_arith");
   }
