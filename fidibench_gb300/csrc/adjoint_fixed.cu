@@ -108,8 +108,8 @@ __device__ __forceinline__ double pow2(int e) {
 // computed, so kNL = kAhead + 2 input planes rotate (z-1, z and the ones
 // being fetched); the forward state F^n (DOTS, int32 in 2^29 units) is
 // staged the same way in kNF = kAhead + 1 buffers.  Without DOTS (the
-// forward recompute) each output value is also stored in 2^29 units in
-// out_hi, the form the contraction reads.
+// batched adjoint's forward recompute) each output value is also stored in
+// 2^29 units in out_hi, the form the contraction reads.
 // Thread (warp w, lane l) owns cells (x = l, y = w*R + r) of the tile.
 constexpr int kAhead = 2;
 constexpr int kNL = kAhead + 2;
