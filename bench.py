@@ -283,8 +283,10 @@ def bench_adjoint(stream) -> dict:
     """Adjoint form: 256^3, v = (0.8, 0.5, -0.6), dt = 0.5 min dx/|v|, 200
     steps, checkpoints every 20; L = 0.5 ||f_T - target||^2 with a seeded
     Gaussian random field target (correlation length 8 cells).  Reports the
-    adjoint/forward per-step cost, the dot-product test and central finite
-    differences (h = 1e-6) on 16 seeded directions and the 3 velocities."""
+    adjoint/forward per-step cost (with dL/dv, and for dL/df0 alone, which
+    is the transposed problem advected without checkpoints), the dot-product
+    test and central finite differences (h = 1e-6) on 16 seeded directions
+    and the 3 velocities."""
     import torch
     import fidibench_gb300 as fdb
 
@@ -328,6 +330,12 @@ def bench_adjoint(stream) -> dict:
         g0, gv = up.adjoint(ADJ_STEPS, dt, lam, checkpoint_every=ADJ_CKPT)
         timings.append(up.adjoint_timings())
     t = timings[-1]
+    # dL/df0 alone: the transposed problem (every upwind direction reversed)
+    for _ in range(2):
+        up.set_field(f0)
+        g0_fast, _ = up.adjoint(ADJ_STEPS, dt, lam, velocity_grad=False)
+        t_fast = up.adjoint_timings()
+    fast_vs_full = float(torch.max(torch.abs(g0_fast - g0)) / torch.max(torch.abs(g0)))
 
     h = 1e-6
 
@@ -369,6 +377,9 @@ def bench_adjoint(stream) -> dict:
             "adjoint_over_forward": adj_step / fwd_ms_step,
             "backward_incl_recompute_over_forward": (adj_step + rec_step) / fwd_ms_step,
             "adjoint_gcups": ADJ_N ** 3 / (adj_step * 1e-3) / 1e9,
+            "f0_only_ms_per_step": t_fast["adjoint_ms"] / ADJ_STEPS,
+            "f0_only_over_forward": t_fast["adjoint_ms"] / ADJ_STEPS / fwd_ms_step,
+            "f0_only_vs_full_rel_maxnorm": fast_vs_full,
             "fd_max_rel_err_f0_16dirs": max(errs_f0), "fd_max_rel_err_velocity": max(errs_v),
             "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "grad_v": [float(x) for x in gv]}
 

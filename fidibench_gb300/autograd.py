@@ -72,8 +72,11 @@ class UpwindAdvect(torch.autograd.Function):
         up.set_field(f0)
         lam = grad_out.detach().to(torch.float64).contiguous().view(-1)
         g0 = torch.empty(f0.numel(), dtype=torch.float64, device=f0.device)
-        g0, gv = up.adjoint(num_steps, dt, lam, g0, checkpoint_every=ck)
-        grad_v = torch.as_tensor(np.asarray(gv), dtype=velocity.dtype, device=velocity.device)
+        # without a velocity gradient the transposed problem alone gives dL/df0
+        want_v = ctx.needs_input_grad[1]
+        g0, gv = up.adjoint(num_steps, dt, lam, g0, checkpoint_every=ck, velocity_grad=want_v)
+        grad_v = (torch.as_tensor(np.asarray(gv), dtype=velocity.dtype, device=velocity.device)
+                  if want_v else None)
         return g0.view_as(f0), grad_v, None, None, None, None
 
 
@@ -150,8 +153,9 @@ class BatchAdvect(torch.autograd.Function):
         b = _batch_handle(shapes, lengths, velocity, f0c.device)
         b.set_fields(f0c)
         lam = grad_out.detach().to(torch.float64).contiguous().view(-1)
-        g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck)
-        grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device)
+        want_v = ctx.needs_input_grad[1]
+        g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck, velocity_grad=want_v)
+        grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device) if want_v else None
         return g0.view_as(grad_out), grad_v, None, None, None, None, None
 
 

@@ -79,14 +79,17 @@ class Batch:
         d = self._dts(dt)
         check(lib.fdb_batch_advect_looped(self._h, int(numTimeSteps), d.ctypes.data))
 
-    def adjoint(self, numTimeSteps: int, dt, lambda_T, grad_f0=None, checkpoint_every: int = 0):
+    def adjoint(self, numTimeSteps: int, dt, lambda_T, grad_f0=None, checkpoint_every: int = 0,
+                velocity_grad: bool = True):
         """Gradients of a loss L(f_T of every instance) given lambda_T =
         dL/df_T: the instances' fields one after another (instance i starts
         at sum(sizes[:i])), a numpy array or a CUDA float64 tensor.  Runs the
         forward steps from the current fields (which end at f_T) and the
         transposed steps backward for all instances at once.  Returns
         (grad_f0 in the same concatenated form and kind, grad_v of shape
-        (count, 3): dL/dv per axis, 0 for missing axes)."""
+        (count, 3): dL/dv per axis, 0 for missing axes).  velocity_grad=False
+        returns (grad_f0, None) from the transposed problems alone (every
+        upwind direction reversed): no checkpoints or recompute."""
         d = self._dts(dt)
         total = sum(self.sizes)
         is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
@@ -105,9 +108,10 @@ class Batch:
             if grad_f0 is None:
                 grad_f0 = np.empty(total, dtype=np.float64)
             lam_p, g_p = lambda_T.ctypes.data, grad_f0.ctypes.data
-        gv = np.zeros((self.count, 3), dtype=np.float64)
+        gv = np.zeros((self.count, 3), dtype=np.float64) if velocity_grad else None
         check(lib.fdb_batch_adjoint(self._h, int(numTimeSteps), d.ctypes.data, lam_p, g_p,
-                                    gv.ctypes.data, int(checkpoint_every), is_dev))
+                                    gv.ctypes.data if velocity_grad else None,
+                                    int(checkpoint_every), is_dev))
         return grad_f0, gv
 
     def checksums(self) -> np.ndarray:

@@ -602,8 +602,7 @@ k_sum3_multi(const double* __restrict__ dpart, const int* __restrict__ cta_base,
 
 }  // namespace
 
-// Geometry of the transposed step: every upwind direction reversed.
-static Geom transposed(const Geom& g) {
+Geom transposed_geom(const Geom& g) {
   Geom t = g;
   t.upz = -g.upz;
   t.upy = -g.upy;
@@ -646,7 +645,7 @@ static int64_t step1_resident() {
 // last wave), at least 4 planes each.  transpose = true: the adjoint (every
 // upwind direction reversed).
 static FixedArgs step1_args(const Geom& g, const Coeffs3& c, bool transpose) {
-  FixedArgs a = make_fixed_args(transpose ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
+  FixedArgs a = make_fixed_args(transpose ? transposed_geom(g) : g, c, fx::kR4W8S, 1, 0,
                                 (int64_t)2 * 152);
   a.tx = 32;
   a.ty = kAR * kAW;
@@ -846,7 +845,7 @@ int batch_adjoint_run(const BatchAdjointIO& io, cudaStream_t st) {
     const Geom& g = io.geoms[i];
     const Coeffs3& c = io.coeffs[i];
     for (int t = 0; t < 2; ++t) {
-      FixedArgs a = make_fixed_args(t == 0 ? transposed(g) : g, c, fx::kR4W8S, 1, 0,
+      FixedArgs a = make_fixed_args(t == 0 ? transposed_geom(g) : g, c, fx::kR4W8S, 1, 0,
                                     (int64_t)2 * 152);
       a.tx = 32;
       a.ty = kAR * kAW;

@@ -357,6 +357,9 @@ struct fdb_batch {
   double* adj_dda = nullptr;
   void* adj_scratch = nullptr;
   size_t adj_scratch_bytes = 0;
+  // plans built while set step the transposed problem (every upwind
+  // direction reversed, the coefficients unchanged): the dL/df0-only adjoint
+  bool transposed_run = false;
   std::vector<int64_t> offsets;  // cells
   std::vector<uint64_t> sizes;
   int64_t total = 0;
@@ -458,7 +461,8 @@ int make_plan(fdb_batch* b, int steps, const double* dt, int K, int shape, int t
     InstDev& I = p->insts[i];
     // per instance: whole z extent per tile unless tz is given (many small
     // instances already fill the device)
-    I.a = make_fixed_args(g, c, shape, K, tz > 0 ? tz : (int)g.nz, resident);
+    I.a = make_fixed_args(b->transposed_run ? transposed_geom(g) : g, c, shape, K,
+                          tz > 0 ? tz : (int)g.nz, resident);
     I.a.scale_log = nullptr;
     I.offset = b->offsets[i];
     const int64_t items = (int64_t)I.a.tiles_x * I.a.tiles_y * I.a.tiles_z;
@@ -515,7 +519,7 @@ int upload_plan(fdb_batch* b, const Plan& p) {
 std::string plan_key(fdb_batch* b, int steps, const double* dt, const Plan& p) {
   std::ostringstream os;
   os << steps << ':' << p.K << ':' << p.shape << ':' << p.tz << ':' << b->cur << ':'
-     << (void*)b->stream;
+     << (void*)b->stream << ':' << b->transposed_run;
   uint64_t h = 1469598103934665603ull;
   for (int i = 0; i < b->count; ++i) {
     uint64_t x;
@@ -895,6 +899,70 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
   return run_looped(b, num_steps, dt, b->K);
 }
 
+// dL/df0 only (fdb_batch_adjoint with grad_v = NULL): the batch advances to
+// f_T, then the persistent launch runs on the adjoint buffers with every
+// upwind direction reversed, (A^T)^S lambda_T for all instances at once.
+static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const double* lambda_T,
+                                 double* grad_f0, int is_device) {
+  const int n = b->count;
+  const size_t T = (size_t)b->total;
+  if (S > 0) FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
+  int rc = FDB_OK;
+  for (auto& p : b->adj_lam)
+    if (!rc && !p) rc = balloc(&p, T);
+  if (!rc && !b->adj_user) rc = balloc(&b->adj_user, T);
+  if (rc) {
+    free_batch_adjoint(b);
+    return rc;
+  }
+  std::vector<uint64_t> pref(n);
+  uint64_t cells = 0;
+  for (int i = 0; i < n; ++i) {
+    pref[i] = cells;
+    cells += b->sizes[i];
+  }
+  const double* lt = lambda_T;
+  if (!is_device) {
+    FDB_CUDA_TRY(cudaMemcpyAsync(b->adj_user, lambda_T, cells * 8, cudaMemcpyHostToDevice,
+                                 b->stream));
+    lt = b->adj_user;
+  }
+  for (int i = 0; i < n; ++i) {
+    double* dst = b->adj_lam[0] + b->offsets[i];
+    if (b->permuted[i])
+      FDB_TRY(launch_permute(b, i, lt + pref[i], dst, false));
+    else
+      FDB_CUDA_TRY(cudaMemcpyAsync(dst, lt + pref[i], b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
+                                   b->stream));
+  }
+  // the persistent launch on the adjoint buffers, transposed problem
+  const int cur = b->cur;
+  std::swap(b->arena[0], b->adj_lam[0]);
+  std::swap(b->arena[1], b->adj_lam[1]);
+  b->cur = 0;
+  b->transposed_run = true;
+  rc = S > 0 ? run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, false) : FDB_OK;
+  const int lc = b->cur;
+  std::swap(b->arena[0], b->adj_lam[0]);
+  std::swap(b->arena[1], b->adj_lam[1]);
+  b->cur = cur;
+  b->transposed_run = false;
+  if (rc) return rc;
+  double* gd = is_device ? grad_f0 : b->adj_user;
+  for (int i = 0; i < n; ++i) {
+    const double* src = b->adj_lam[lc] + b->offsets[i];
+    if (b->permuted[i])
+      FDB_TRY(launch_permute(b, i, src, gd + pref[i], true));
+    else
+      FDB_CUDA_TRY(cudaMemcpyAsync(gd + pref[i], src, b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
+                                   b->stream));
+  }
+  if (!is_device)
+    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, b->adj_user, cells * 8, cudaMemcpyDeviceToHost,
+                                 b->stream));
+  return bsync(b);
+}
+
 int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
                       double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
   FDB_TRY(bcheck(b));
@@ -908,6 +976,7 @@ int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const doubl
   if (K > std::max(S, 1)) K = std::max(S, 1);
   const int nseg = (S + K - 1) / K;
   const int n = b->count;
+  if (!grad_v) return batch_adjoint_f0_only(b, S, dt, lambda_T, grad_f0, is_device);
   // every instance in the fixed kernel's domain (forward and transposed steps)
   std::vector<Coeffs3> cs(n);
   for (int i = 0; i < n; ++i) {

@@ -461,6 +461,61 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   const int arith = fixed ? FDB_ARITH_FIXED
                           : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
 
+  if (!grad_v) {
+    // dL/df0 only: grad_f0 = (A^T)^S lambda_T.  A^T is the upwind step with
+    // every direction reversed and the same Courant numbers, so the forward
+    // kernels on the transposed geometry (with the coefficients of g) apply
+    // it: no checkpoints, no recompute, no contraction.  The field is
+    // advanced to f_T as in the full path.
+    cudaEvent_t t0, t1, t2;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventCreate(&t2);
+    cudaEventRecord(t0, h->stream);
+    FDB_TRY(advance(h, S, dt, arith));
+    cudaEventRecord(t1, h->stream);
+    if (!h->lam[0]) {
+      int rc = dalloc(&h->lam[0], g.ntot);
+      if (!rc) rc = dalloc(&h->lam[1], g.ntot);
+      if (rc) {
+        free_adjoint(h);
+        return rc;
+      }
+    }
+    FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[0], lambda_T, bytes,
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 h->stream));
+    const Geom gT = transposed_geom(g);
+    double* lb[2] = {h->lam[0], h->lam[1]};
+    int lc = 0;
+    if (arith == FDB_ARITH_FIXED) {
+      FixedTuning t = h->tune;
+      t.depth = h->depth;
+      FDB_TRY(launch_advect_fixed_ex(gT, c, S, t, lb, &lc, h->scratch, h->scratch_bytes, nullptr,
+                                     h->stream));
+      h->scale_slot = -1;  // the scratch slots now describe lambda, not the field
+    } else {
+      for (int k = 0; k < S; ++k) {
+        FDB_TRY(launch_step_f64(gT, c, arith, lb[lc], lb[lc ^ 1], h->stream));
+        lc ^= 1;
+      }
+    }
+    cudaEventRecord(t2, h->stream);
+    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, lb[lc], bytes,
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 h->stream));
+    const int rc = sync(h);
+    float ms = 0.f;
+    h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
+    if (cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess) h->adj_ms[0] = ms;
+    if (cudaEventElapsedTime(&ms, t1, t2) == cudaSuccess) h->adj_ms[2] = ms;
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaEventDestroy(t2);
+    cudaGetLastError();
+    return rc;
+  }
+
   // storage: nseg checkpoints, the segment's states (FP64: K - 1 buffers;
   // fixed point: two int64 chain buffers and K int32 arrays), two adjoint
   // buffers

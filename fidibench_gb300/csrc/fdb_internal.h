@@ -60,6 +60,10 @@ int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Ge
 // The reference coefficient of axis j: ((dt * v_j) * up_j) / dx_j  (upwind.cxx:72).
 double ref_coeff(const Geom& g, int j, double dt);
 
+// The geometry of the transposed step: every upwind direction reversed
+// (with the coefficients of g, the step on it is A^T).
+Geom transposed_geom(const Geom& g);
+
 // Step coefficients in the 3-D view.  c* are the reference coefficients
 // (c <= 0); a* = -c* are the Courant numbers; w = ((1 - a_z) - a_y) - a_x.
 struct Coeffs3 {
@@ -130,8 +134,8 @@ struct AdjointFixedIO {
   int nseg;   // ceil(S / K)
   double* const* ckpt;
   // recomputed segment: its states march through two int64 buffers; the
-  // contraction reads each state's values rounded to 2^32 units, kept as
-  // int32 (K arrays of ntot)
+  // contraction reads each state in 2^29 units, kept as int32 (K arrays of
+  // ntot)
   int64_t* chain[2];
   int32_t* const* state_hi;
   int64_t* lam[2];         // adjoint ping-pong (int64)

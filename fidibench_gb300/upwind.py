@@ -201,13 +201,15 @@ class Upwind:
 
     # -- adjoint -------------------------------------------------------------------
     def adjoint(self, numTimeSteps: int, deltaTime: float, lambda_T, grad_f0=None,
-                checkpoint_every: int = 0):
+                checkpoint_every: int = 0, velocity_grad: bool = True):
         """Gradient of a loss L(f_T) given lambda_T = dL/df_T.
 
         Runs the forward steps from the current field (which ends at f_T) and
         the transposed steps backward with checkpoint/recompute.  Returns
         (grad_f0, grad_v).  lambda_T/grad_f0 may be numpy arrays or CUDA
-        tensors (both of the same kind)."""
+        tensors (both of the same kind).  velocity_grad=False returns
+        (grad_f0, None) from the transposed problem alone (every upwind
+        direction reversed): no checkpoints or recompute."""
         is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
         if is_dev:
             _order_after_torch(lambda_T)
@@ -219,11 +221,12 @@ class Upwind:
                 grad_f0 = np.empty(self.ntot, dtype=np.float64)
         if not is_dev:
             lambda_T = _as_f64(lambda_T).reshape(-1)
-        gv = np.zeros(self.ndims, dtype=np.float64)
+        gv = np.zeros(self.ndims, dtype=np.float64) if velocity_grad else None
         if not is_dev:
             grad_f0 = np.ascontiguousarray(grad_f0, dtype=np.float64)
         check(lib.fdb_upwind_adjoint(self._h, int(numTimeSteps), float(deltaTime),
-                                     _capi.dptr(lambda_T), _capi.dptr(grad_f0), gv.ctypes.data,
+                                     _capi.dptr(lambda_T), _capi.dptr(grad_f0),
+                                     gv.ctypes.data if velocity_grad else None,
                                      int(checkpoint_every), is_dev))
         return grad_f0, gv
 

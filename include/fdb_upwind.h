@@ -138,6 +138,10 @@ int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius,
  * each segment from its checkpoint.  Writes grad_f0 = dL/df0 (ntot values)
  * and grad_v = dL/dv (ndims values, host memory).  The handle's field is left
  * at f_T (as after advect).  Pointers are device memory when is_device = 1.
+ * With grad_v = NULL only dL/df0 = (A^T)^S lambda_T is computed, by the
+ * forward kernels on the problem with every upwind direction reversed (the
+ * transpose of the step): no checkpoints, recompute or contraction, about the
+ * cost of an advect; it agrees with the full path to rounding (1e-13).
  * ------------------------------------------------------------------------- */
 int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
                        const double* lambda_T, double* grad_f0, double* grad_v,
@@ -207,7 +211,9 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt);
  * instances 0..i-1); grad_v receives 3 values per instance (dL/dv per
  * reference axis, 0 for missing axes; host memory); dt holds one time step
  * per instance; checkpoint_every as in fdb_upwind_adjoint.  The batch's fields
- * are left at f_T.  Field pointers are device memory when is_device = 1. */
+ * are left at f_T.  Field pointers are device memory when is_device = 1.
+ * With grad_v = NULL only dL/df0 is computed: the persistent launch on the
+ * problems with every upwind direction reversed (as in fdb_upwind_adjoint). */
 int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
                       double* grad_f0, double* grad_v, int checkpoint_every, int is_device);
 /* checksum() of every instance (upwind.cxx:91-93) into out[count]; synchronises. */

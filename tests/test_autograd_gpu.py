@@ -69,3 +69,20 @@ def test_batch_advect_fn_matches_single_field(fdb):
         got = out[off:off + f.numel()]
         assert torch.max(torch.abs(got - ref)) <= 1e-13 * torch.max(torch.abs(ref))
         off += f.numel()
+
+
+def test_gradcheck_f0_only(fdb):
+    """With the velocity not requiring grad, both Functions take dL/df0 from
+    the transposed problem alone; torch's gradcheck still holds."""
+    import torch
+    from fidibench_gb300.autograd import BatchAdvect, UpwindAdvect
+    f0 = torch.rand((3, 4, 5), dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor([0.6, -0.4, 0.3], dtype=torch.float64)
+    fn = lambda f: UpwindAdvect.apply(f, v, 3, 0.05, (1.0, 1.0, 1.0), 0)  # noqa: E731
+    assert torch.autograd.gradcheck(fn, (f0,), eps=1e-6, atol=1e-8, rtol=1e-6)
+    shapes = ((3, 4, 5), (4, 3))
+    lengths = ((1.0, 1.0, 1.0), (1.0, 2.0))
+    fb = torch.rand(72, dtype=torch.float64, device="cuda", requires_grad=True)
+    vb = torch.tensor([[0.6, -0.4, 0.3], [-0.5, 0.7, 0.0]], dtype=torch.float64)
+    fnb = lambda f: BatchAdvect.apply(f, vb, shapes, lengths, 3, (0.05, 0.04), 0)  # noqa: E731
+    assert torch.autograd.gradcheck(fnb, (fb,), eps=1e-6, atol=1e-8, rtol=1e-6)

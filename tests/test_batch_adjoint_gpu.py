@@ -192,3 +192,28 @@ def test_batch_set_velocity(fdb):
         assert rel_maxnorm(b.get_field(k), up.f) <= 1e-13, k
         up.close()
     b.close()
+
+
+def test_batch_f0_only_adjoint(fdb):
+    """velocity_grad=False on a batch: the persistent launch on the
+    transposed problems agrees with the full batched adjoint and leaves the
+    fields at f_T."""
+    rng = np.random.default_rng(37)
+    dts = _dts(SPECS)
+    f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in SPECS]
+    lam = np.concatenate([rng.standard_normal(x.size) for x in f0])
+    b = _batch(fdb, SPECS, f0)
+    b.advect(19, dts)
+    ft = [b.get_field(k) for k in range(len(SPECS))]  # one advect call, as the fast path
+    for k, f in enumerate(f0):
+        b.set_field(k, f)
+    g_full, _ = b.adjoint(19, dts, lam, checkpoint_every=6)
+    for k, f in enumerate(f0):
+        b.set_field(k, f)
+    g_fast, gv = b.adjoint(19, dts, lam, velocity_grad=False)
+    assert gv is None
+    off = np.cumsum([0] + [x.size for x in f0])
+    for k in range(len(SPECS)):
+        assert rel_maxnorm(g_fast[off[k]:off[k + 1]], g_full[off[k]:off[k + 1]]) <= 1e-13, k
+        assert np.array_equal(b.get_field(k), ft[k]), k
+    b.close()
