@@ -705,30 +705,34 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       cudaEventCreate(&e2);
       cudaEventRecord(e0, st);
     }
-    // states f^{sK} .. f^{sK+len-1}: state 0 from the checkpoint (forward
-    // ring position 0), then the temporally blocked forward kernel, kRec
-    // steps per launch, which stores every level in state_g units; the int64
-    // chain ping-pongs between the two chain buffers
-    k_ring_init<<<1, 32, 0, st>>>(fr);
-    k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], n, fr);
-    k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], n, fr,
-                                           fr + 1, fr + 2, gK, logs + 0, err);
-    note_launch(3);
-    int cc = 0;   // chain buffer of the latest state
-    int pos = 1;  // forward ring position of the next launch
-    for (int k = 1; k < len;) {
-      const int kb = std::min(kRec, len - k);
-      FDB_TRY(launch_fixed_one(g, c, fx::kR4W8S, kb, io.chain[cc], io.chain[cc ^ 1], false, false,
-                               fr, pos, err, 0, kRec, logs + k, st, io.state_hi + k));
-      cc ^= 1;
-      ++pos;
-      k += kb;
+    {
+      NvtxScope nvtx_r("fdb.adjoint.recompute");
+      // states f^{sK} .. f^{sK+len-1}: state 0 from the checkpoint (forward
+      // ring position 0), then the temporally blocked forward kernel, kRec
+      // steps per launch, which stores every level in state_g units; the int64
+      // chain ping-pongs between the two chain buffers
+      k_ring_init<<<1, 32, 0, st>>>(fr);
+      k_absmax_slot<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], n, fr);
+      k_to_fixed<<<grid_for(n), 256, 0, st>>>(io.ckpt[sgi], io.chain[0], io.state_hi[0], n, fr,
+                                             fr + 1, fr + 2, gK, logs + 0, err);
+      note_launch(3);
+      int cc = 0;   // chain buffer of the latest state
+      int pos = 1;  // forward ring position of the next launch
+      for (int k = 1; k < len;) {
+        const int kb = std::min(kRec, len - k);
+        FDB_TRY(launch_fixed_one(g, c, fx::kR4W8S, kb, io.chain[cc], io.chain[cc ^ 1], false,
+                                 false, fr, pos, err, 0, kRec, logs + k, st, io.state_hi + k));
+        cc ^= 1;
+        ++pos;
+        k += kb;
+      }
     }
     FDB_CUDA_TRY(cudaGetLastError());
     if (io.recompute_ev) {
       cudaEventRecord(e1, st);
       io.recompute_ev->push_back({e0, e1});
     }
+    NvtxScope nvtx_t("fdb.adjoint.transposed");
     // adjoint steps n = sK+len-1 .. sK
     for (int k = len - 1; k >= 0; --k) {
       aT.slot_in = lr + (li % 3);

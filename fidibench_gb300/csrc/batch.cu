@@ -879,6 +879,7 @@ int fdb_batch_set_tuning(fdb_batch* b, int key, int value) {
 }
 
 int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt) {
+  NvtxScope nvtx_("fdb.batch.advect");
   FDB_TRY(bcheck(b));
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   FDB_TRY(check_dts(b, dt));
@@ -892,6 +893,7 @@ int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt) {
 }
 
 int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
+  NvtxScope nvtx_("fdb.batch.advect_looped");
   FDB_TRY(bcheck(b));
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   FDB_TRY(check_dts(b, dt));
@@ -965,6 +967,7 @@ static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const do
 
 int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
                       double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
+  NvtxScope nvtx_("fdb.batch.adjoint");
   FDB_TRY(bcheck(b));
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   FDB_TRY(check_dts(b, dt));

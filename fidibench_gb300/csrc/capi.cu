@@ -313,6 +313,7 @@ int fdb_upwind_field_ptr(fdb_upwind* h, double** out) {
 }
 
 int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt) {
+  NvtxScope nvtx_("fdb.advect");
   FDB_TRY(check_handle(h));
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
@@ -439,6 +440,7 @@ int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
 
 int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* lambda_T,
                        double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
+  NvtxScope nvtx_("fdb.adjoint");
   FDB_TRY(check_handle(h));
   const Geom& g = h->g;
   if (g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "adjoint serves ndims <= 3");
@@ -541,11 +543,14 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   cudaEventCreate(&fe0);
   cudaEventCreate(&fe1);
   cudaEventRecord(fe0, h->stream);
-  for (int s = 0; s < nseg; ++s) {
-    FDB_CUDA_TRY(cudaMemcpyAsync(h->ckpt[s], h->buf[h->cur], bytes, cudaMemcpyDeviceToDevice,
-                                 h->stream));
-    const int len = std::min(K, S - s * K);
-    FDB_TRY(advance(h, len, dt, arith));
+  {
+    NvtxScope nvtx_f("fdb.adjoint.forward");
+    for (int s = 0; s < nseg; ++s) {
+      FDB_CUDA_TRY(cudaMemcpyAsync(h->ckpt[s], h->buf[h->cur], bytes, cudaMemcpyDeviceToDevice,
+                                   h->stream));
+      const int len = std::min(K, S - s * K);
+      FDB_TRY(advance(h, len, dt, arith));
+    }
   }
   cudaEventRecord(fe1, h->stream);
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rec_ev, adj_ev;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -36,6 +37,16 @@ bool fault_injected(const char* kind);
 // Launch accounting behind fdb_launch_count(): every launch wrapper adds the
 // number of kernels it enqueued.
 void note_launch(uint64_t n = 1);
+
+// NVTX range for the lifetime of a scope (names the library's phases in
+// profiler timelines and lets ncu filter captures by phase, e.g.
+// `ncu --nvtx --nvtx-include "fdb.adjoint.transposed/"`; no cost without a tool).
+struct NvtxScope {
+  explicit NvtxScope(const char* name) { nvtxRangePushA(name); }
+  ~NvtxScope() { nvtxRangePop(); }
+  NvtxScope(const NvtxScope&) = delete;
+  NvtxScope& operator=(const NvtxScope&) = delete;
+};
 
 // Geometry of one problem, normalised to 3 internal axes (z, y, x) = reference
 // axes (ndims-3, ndims-2, ndims-1); missing leading axes have extent 1 and

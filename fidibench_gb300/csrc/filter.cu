@@ -356,6 +356,7 @@ int fdb_filter_get_data(fdb_filter* f, int which, double* dst, int is_device) {
 }
 
 int fdb_filter_apply(fdb_filter* f) {
+  fdb::NvtxScope nvtx_("fdb.filter.apply");
   FDB_TRY(check(f));
   return launch_apply(f);
 }
@@ -368,6 +369,7 @@ int fdb_filter_copy_out_to_in(fdb_filter* f) {
 }
 
 int fdb_filter_iterate(fdb_filter* f, int iterations) {
+  fdb::NvtxScope nvtx_("fdb.filter.iterate");
   FDB_TRY(check(f));
   if (iterations < 0) return fail(FDB_ERR_INVALID, "iterations must be >= 0");
   for (int k = 0; k < iterations; ++k) {
