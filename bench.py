@@ -13,7 +13,10 @@ field = sphere indicator (centre 0.5^3, radius 0.2) + seeded uniform noise in
                larger than L2, so no flush is needed between steps).
   e2e          the same metric through the public API with host buffers:
                every step uploads the initial field from pinned host memory,
-               advects, downloads the field and reads the checksum.
+               advects, downloads the field and reads the checksum
+               (Upwind.advect_host_stream: the next upload and the previous
+               download overlap each advect).  `serial_value` is the same
+               cycle as separate set_field/advect/get_field/checksum calls.
   roofline     the step kernel's achieved bandwidth on the 16 B/cell-update
                algorithmic basis (read f once, write f once) against the
                measured HBM copy peak.
@@ -581,26 +584,38 @@ def main() -> None:
         host_in = torch.empty(int(cells), dtype=torch.float64, pin_memory=True)
         host_out = torch.empty(int(cells), dtype=torch.float64, pin_memory=True)
         up.get_field(host_in)  # a real field as input
-        for _ in range(2):
+
+        def serial_cycle():
             up.set_field(host_in)
             up.advect(TIME_STEPS, DT)
             up.get_field(host_out)
             up.checksum()
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            up.set_field(host_in)
-            up.advect(TIME_STEPS, DT)
-            up.get_field(host_out)
-            up.checksum()
-        barrier()
-        el = time.perf_counter() - t0
-        te = torch.tensor([el], device="cuda", dtype=torch.float64)
-        if dist is not None:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        el = float(te.item())
+
+        def timed(fn):
+            barrier()
+            t = time.perf_counter()
+            fn()
+            barrier()
+            el = time.perf_counter() - t
+            te = torch.tensor([el], device="cuda", dtype=torch.float64)
+            if dist is not None:
+                dist.all_reduce(te, op=dist.ReduceOp.MAX)
+            return float(te.item())
+
+        # the public streaming call: every step uploads its field, advects,
+        # downloads the result and returns its checksum; the next upload and
+        # the previous download overlap each advect
+        up.advect_host_stream([host_in] * 2, TIME_STEPS, DT, out=[host_out] * 2)
+        el = timed(lambda: up.advect_host_stream([host_in] * args.steps, TIME_STEPS, DT,
+                                                 out=[host_out] * args.steps))
+        # the same cycle one call after another (copies not overlapped)
+        serial_cycle()
+        el_serial = timed(lambda: [serial_cycle() for _ in range(args.steps)])
         e2e = {"value": ws * cells * TIME_STEPS * args.steps / el / 1e9, "unit": "GCUPS",
-               "h2d_bytes_per_step": int(cells) * 8, "d2h_bytes_per_step": int(cells) * 8 + 8}
+               "h2d_bytes_per_step": int(cells) * 8, "d2h_bytes_per_step": int(cells) * 8 + 8,
+               "api": "Upwind.advect_host_stream (fdb_upwind_advect_host_stream)",
+               "serial_value": ws * cells * TIME_STEPS * args.steps / el_serial / 1e9,
+               "serial_api": "set_field + advect + get_field + checksum per step"}
     up.close()
 
     batched = None

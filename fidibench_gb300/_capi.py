@@ -47,6 +47,8 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_field_ptr": (_int, [_vp, ctypes.POINTER(_vp)]),
     "fdb_upwind_advect": (_int, [_vp, _int, ctypes.c_double]),
     "fdb_upwind_checksum": (_int, [_vp, _dp]),
+    "fdb_upwind_advect_host_stream": (_int, [_vp, _int, _vp, _vp, _int, ctypes.c_double, _vp]),
+    "fdb_upwind_advect_transposed": (_int, [_vp, _int, ctypes.c_double, _vp, _vp, _int]),
     "fdb_upwind_std": (_int, [_vp, _dp]),
     "fdb_upwind_set_stream": (_int, [_vp, _vp]),
     "fdb_upwind_set_velocity": (_int, [_vp, _vp]),
@@ -59,6 +61,7 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_batch_count": (_int, [_vp, ctypes.POINTER(_int), _u64p]),
     "fdb_batch_storage_order": (_int, [_vp, _int, ctypes.POINTER(_int)]),
     "fdb_batch_adjoint": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _int, _int]),
+    "fdb_batch_advect_transposed": (_int, [_vp, _int, _vp, _vp, _vp, _int]),
     "fdb_batch_set_velocity": (_int, [_vp, _int, _vp]),
     "fdb_batch_set_field": (_int, [_vp, _int, _vp, _int]),
     "fdb_batch_get_field": (_int, [_vp, _int, _vp, _int]),

@@ -8,6 +8,8 @@ fastest, as in upwind/cxx/upwind.cxx:39-44); velocity is a float64 tensor of
 ndims values.  Gradients flow to both: dL/df0 from the transposed steps and
 dL/dv from the per-step coefficient contractions (the upwind direction is
 piecewise constant in v, so dv is the derivative within the sign pattern).
+When the velocity needs no gradient, the backward pass is the transposed
+problem alone (fdb_upwind_advect_transposed): the forward is not re-run.
 torch supplies only device memory and the autograd graph; every step runs in
 libfdb_upwind.  batch_advect_fn does the same for many instances at once
 (fdb_batch_advect forward, fdb_batch_adjoint backward).
@@ -69,14 +71,16 @@ class UpwindAdvect(torch.autograd.Function):
         v = velocity.to("cpu", torch.float64).numpy().copy()
         up = _handle(f0.shape, lengths, v, f0.device)
         torch.cuda.current_stream(f0.device).synchronize()
-        up.set_field(f0)
         lam = grad_out.detach().to(torch.float64).contiguous().view(-1)
         g0 = torch.empty(f0.numel(), dtype=torch.float64, device=f0.device)
-        # without a velocity gradient the transposed problem alone gives dL/df0
-        want_v = ctx.needs_input_grad[1]
-        g0, gv = up.adjoint(num_steps, dt, lam, g0, checkpoint_every=ck, velocity_grad=want_v)
-        grad_v = (torch.as_tensor(np.asarray(gv), dtype=velocity.dtype, device=velocity.device)
-                  if want_v else None)
+        if not ctx.needs_input_grad[1]:
+            # without a velocity gradient dL/df0 = (A^T)^S lam alone: the
+            # transposed problem, no re-run of the forward
+            up.advect_transposed(num_steps, dt, lam, g0)
+            return g0.view_as(f0), None, None, None, None, None
+        up.set_field(f0)
+        g0, gv = up.adjoint(num_steps, dt, lam, g0, checkpoint_every=ck)
+        grad_v = torch.as_tensor(np.asarray(gv), dtype=velocity.dtype, device=velocity.device)
         return g0.view_as(f0), grad_v, None, None, None, None
 
 
@@ -128,7 +132,8 @@ class BatchAdvect(torch.autograd.Function):
     (count, 3) float64 tensor (row i: the instance's velocity, zero-padded
     beyond its axes), dts one time step per instance.  Forward: the batch's
     persistent advect; backward: fdb_batch_adjoint, giving dL/df0 and dL/dv
-    for all instances at once."""
+    for all instances at once (fdb_batch_advect_transposed alone when the
+    velocity needs no gradient)."""
 
     @staticmethod
     def forward(ctx, f0, velocity, shapes, lengths, num_steps: int, dts,
@@ -151,11 +156,14 @@ class BatchAdvect(torch.autograd.Function):
         f0c, velocity = ctx.saved_tensors
         shapes, lengths, num_steps, dts, ck = ctx.meta
         b = _batch_handle(shapes, lengths, velocity, f0c.device)
-        b.set_fields(f0c)
         lam = grad_out.detach().to(torch.float64).contiguous().view(-1)
-        want_v = ctx.needs_input_grad[1]
-        g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck, velocity_grad=want_v)
-        grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device) if want_v else None
+        if not ctx.needs_input_grad[1]:
+            # dL/df0 alone: the transposed problems, no re-run of the forward
+            g0 = b.advect_transposed(num_steps, dts, lam)
+            return g0.view_as(grad_out), None, None, None, None, None, None
+        b.set_fields(f0c)
+        g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck)
+        grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device)
         return g0.view_as(grad_out), grad_v, None, None, None, None, None
 
 

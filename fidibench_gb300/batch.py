@@ -114,6 +114,33 @@ class Batch:
                                     int(checkpoint_every), is_dev))
         return grad_f0, gv
 
+    def advect_transposed(self, numTimeSteps: int, dt, values, out=None):
+        """(A^T)^S applied to every instance of ``values`` (concatenated as
+        in adjoint(), numpy or CUDA float64 tensor) without touching the
+        fields: the grad_f0 of adjoint(velocity_grad=False), for callers that
+        already hold f_T.  ``out`` may be ``values``."""
+        d = self._dts(dt)
+        total = sum(self.sizes)
+        is_dev = 1 if getattr(values, "is_cuda", False) else 0
+        if is_dev:
+            import torch
+            torch.cuda.current_stream(values.device).synchronize()  # torch's writes first
+            if values.numel() != total:
+                raise ValueError(f"values need {total} entries, got {values.numel()}")
+            if out is None:
+                out = torch.empty(total, dtype=torch.float64, device=values.device)
+            in_p, out_p = values.data_ptr(), out.data_ptr()
+        else:
+            values = np.ascontiguousarray(np.asarray(values, dtype=np.float64)).reshape(-1)
+            if values.size != total:
+                raise ValueError(f"values need {total} entries, got {values.size}")
+            if out is None:
+                out = np.empty(total, dtype=np.float64)
+            in_p, out_p = values.ctypes.data, out.ctypes.data
+        check(lib.fdb_batch_advect_transposed(self._h, int(numTimeSteps), d.ctypes.data, in_p,
+                                              out_p, is_dev))
+        return out
+
     def checksums(self) -> np.ndarray:
         out = np.empty(self.count, dtype=np.float64)
         check(lib.fdb_batch_checksums(self._h, out.ctypes.data))

@@ -901,14 +901,13 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
   return run_looped(b, num_steps, dt, b->K);
 }
 
-// dL/df0 only (fdb_batch_adjoint with grad_v = NULL): the batch advances to
-// f_T, then the persistent launch runs on the adjoint buffers with every
-// upwind direction reversed, (A^T)^S lambda_T for all instances at once.
-static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const double* lambda_T,
-                                 double* grad_f0, int is_device) {
+// out = (A^T)^S in for all instances at once: the persistent launch on the
+// adjoint buffers with every upwind direction reversed; the fields are
+// untouched.
+static int batch_transposed(fdb_batch* b, int S, const double* dt, const double* lambda_T,
+                            double* grad_f0, int is_device) {
   const int n = b->count;
   const size_t T = (size_t)b->total;
-  if (S > 0) FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
   int rc = FDB_OK;
   for (auto& p : b->adj_lam)
     if (!rc && !p) rc = balloc(&p, T);
@@ -963,6 +962,24 @@ static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const do
     FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, b->adj_user, cells * 8, cudaMemcpyDeviceToHost,
                                  b->stream));
   return bsync(b);
+}
+
+// dL/df0 only (fdb_batch_adjoint with grad_v = NULL): the batch advances to
+// f_T, then the transposed launch gives (A^T)^S lambda_T.
+static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const double* lambda_T,
+                                 double* grad_f0, int is_device) {
+  if (S > 0) FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
+  return batch_transposed(b, S, dt, lambda_T, grad_f0, is_device);
+}
+
+int fdb_batch_advect_transposed(fdb_batch* b, int num_steps, const double* dt, const double* in,
+                                double* out, int is_device) {
+  NvtxScope nvtx_("fdb.batch.advect_transposed");
+  FDB_TRY(bcheck(b));
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  FDB_TRY(check_dts(b, dt));
+  if (!in || !out) return fail(FDB_ERR_INVALID, "null input or output");
+  return batch_transposed(b, num_steps, dt, in, out, is_device);
 }
 
 int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,

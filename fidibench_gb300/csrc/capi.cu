@@ -44,6 +44,15 @@ struct fdb_upwind {
   double* adj_scratch = nullptr;
   size_t adj_scratch_bytes = 0;
   double adj_ms[3] = {0.0, 0.0, 0.0};  // last adjoint: forward, recompute, transposed steps
+  // fdb_upwind_advect_host_stream: a third field buffer (the three rotate
+  // between upload, advect pair and download), the upload and download
+  // streams and their events (two of each kind, alternating by field parity)
+  double* extra = nullptr;
+  // the transposed problem's own max|f| slots and error word, so that a
+  // transposed run leaves the field's scale slot valid
+  double* tscratch = nullptr;
+  cudaStream_t io_stream[2] = {nullptr, nullptr};
+  cudaEvent_t io_ev[7] = {};
 };
 
 namespace fdb {
@@ -138,18 +147,27 @@ int check_handle(fdb_upwind* h) {
   return FDB_OK;
 }
 
-// Synchronise the handle's stream and report the device error word that the
-// fixed-point kernels set when they meet a non-finite input.
-int sync(fdb_upwind* h) {
-  FDB_CUDA_TRY(cudaStreamSynchronize(h->stream));
-  int* err = fixed_error_word(h->scratch);
+// Report (and clear) the error word that the fixed-point kernels set in a
+// scratch block when they meet a non-finite input.  The stream must be
+// synchronised.
+int check_error_word(double* scratch, const char* what) {
+  int* err = fixed_error_word(scratch);
   int herr = 0;
   FDB_CUDA_TRY(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
   if (herr) {
     FDB_CUDA_TRY(cudaMemset(err, 0, sizeof(int)));
-    return fail(FDB_ERR_NONFINITE,
-                "the field holds NaN or Inf values (the fixed-point kernel needs finite input)");
+    return fail(FDB_ERR_NONFINITE, std::string(what) +
+                                       " holds NaN or Inf values (the fixed-point kernel needs "
+                                       "finite input)");
   }
+  return FDB_OK;
+}
+
+// Synchronise the handle's stream and report a non-finite field.
+int sync(fdb_upwind* h) {
+  FDB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  FDB_TRY(check_error_word(h->scratch, "the field"));
+  if (h->tscratch) FDB_TRY(check_error_word(h->tscratch, "the transposed input"));
   return FDB_OK;
 }
 
@@ -191,6 +209,19 @@ int resolve_arith(fdb_upwind* h, const Coeffs3& c) {
   return (ok && fixed_preferred(g)) ? FDB_ARITH_FIXED : FDB_ARITH_FMA;
 }
 
+// The arithmetic an advect by dt uses (FDB_ERR_UNSUPPORTED when FIXED was
+// forced outside its domain).
+int pick_arith(fdb_upwind* h, double dt, int* arith) {
+  *arith = FDB_ARITH_EXACT;
+  if (h->g.ndims > 3) return FDB_OK;  // generic kernel
+  *arith = resolve_arith(h, coeffs3(h->g, dt));
+  if (*arith < 0)
+    return fail(FDB_ERR_UNSUPPORTED,
+                "FDB_ARITH_FIXED requested but the geometry/coefficients are outside its "
+                "domain (see fdb_upwind_set_arith)");
+  return FDB_OK;
+}
+
 // Advance the handle's field by `steps` steps with the given arithmetic.
 int advance(fdb_upwind* h, int steps, double dt, int arith) {
   const Geom& g = h->g;
@@ -213,6 +244,137 @@ int advance(fdb_upwind* h, int steps, double dt, int arith) {
   for (int s = 0; s < steps; ++s) {
     FDB_TRY(launch_step_f64(g, c, arith, h->buf[h->cur], h->buf[h->cur ^ 1], h->stream));
     h->cur ^= 1;
+  }
+  return FDB_OK;
+}
+
+// A CUDA event that lives as long as its scope.
+struct ScopedEvent {
+  cudaEvent_t e = nullptr;
+  ScopedEvent() { cudaEventCreate(&e); }
+  ~ScopedEvent() {
+    if (e) cudaEventDestroy(e);
+  }
+  ScopedEvent(const ScopedEvent&) = delete;
+  ScopedEvent& operator=(const ScopedEvent&) = delete;
+};
+
+// The arithmetic of the adjoint and of transposed runs: the fixed-point
+// kernels where the handle's settings allow them and the coefficients are in
+// their domain, else the FP64 kernel the handle asks for.
+int adjoint_arith(fdb_upwind* h, const Coeffs3& c) {
+  const bool fixed = (h->arith == FDB_ARITH_AUTO || h->arith == FDB_ARITH_FIXED) &&
+                     fixed_supported(h->g, c, 1) == FDB_OK &&
+                     fixed_supported(h->g, c, h->depth) == FDB_OK;
+  return fixed ? FDB_ARITH_FIXED
+               : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
+}
+
+// out = (A^T)^S in.  A^T is the upwind step with every direction reversed and
+// the same Courant numbers, so the forward kernels on the transposed geometry
+// (with the coefficients of g) apply it.  Runs through the handle's adjoint
+// buffers with its own scale scratch: the field, its buffers and its scale
+// slot are untouched.  t_done (nullable) is recorded after the last step.
+int transposed_run(fdb_upwind* h, int S, double dt, const double* in, double* out,
+                   int is_device, cudaEvent_t t_done) {
+  const Geom& g = h->g;
+  const size_t bytes = g.ntot * sizeof(double);
+  const Coeffs3 c = coeffs3(g, dt);
+  const int arith = adjoint_arith(h, c);
+  if (!h->lam[0]) {
+    int rc = dalloc(&h->lam[0], g.ntot);
+    if (!rc) rc = dalloc(&h->lam[1], g.ntot);
+    if (rc) {
+      free_adjoint(h);
+      return rc;
+    }
+  }
+  if (!h->tscratch) {
+    FDB_TRY(dalloc(&h->tscratch, (fixed_scratch_bytes() + 7) / 8));
+    FDB_CUDA_TRY(cudaMemsetAsync(h->tscratch, 0, h->scratch_bytes, h->stream));
+  }
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[0], in, bytes,
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               h->stream));
+  const Geom gT = transposed_geom(g);
+  double* lb[2] = {h->lam[0], h->lam[1]};
+  int lc = 0;
+  if (arith == FDB_ARITH_FIXED) {
+    FixedTuning t = h->tune;
+    t.depth = h->depth;
+    FDB_TRY(launch_advect_fixed_ex(gT, c, S, t, lb, &lc, h->tscratch, h->scratch_bytes, nullptr,
+                                   h->stream));
+  } else {
+    for (int k = 0; k < S; ++k) {
+      FDB_TRY(launch_step_f64(gT, c, arith, lb[lc], lb[lc ^ 1], h->stream));
+      lc ^= 1;
+    }
+  }
+  if (t_done) FDB_CUDA_TRY(cudaEventRecord(t_done, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(out, lb[lc], bytes,
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  return FDB_OK;
+}
+
+// Buffers and streams of fdb_upwind_advect_host_stream, created on first use.
+int ensure_host_stream(fdb_upwind* h) {
+  if (!h->extra) FDB_TRY(dalloc(&h->extra, h->g.ntot));
+  for (cudaStream_t& s : h->io_stream)
+    if (!s) FDB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : h->io_ev)
+    if (!e) FDB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return FDB_OK;
+}
+
+// The three field buffers of the host stream and the role each plays now:
+// `in` holds the field about to advect, `other` is its ping-pong partner and
+// `third` receives the next upload (it held the previous result, whose
+// download must end first).  The roles rotate after every field; the three
+// pointers never change.
+struct FieldRing {
+  double* d[3];
+  int in, other, third;
+};
+
+// Enqueue the whole host stream.  Event slots: 0 = start, 1 + p = field
+// uploaded, 3 + p = field advected and summed, 5 + p = field downloaded, with
+// p the parity of the field (a wait binds to the record made before it, so
+// two slots per kind suffice).
+int host_stream_enqueue(fdb_upwind* h, int count, const double* const* in, double* const* out,
+                        int num_steps, double dt, int arith, double* dsum, FieldRing& r) {
+  const size_t bytes = h->g.ntot * sizeof(double);
+  cudaStream_t cs = h->stream, up = h->io_stream[0], down = h->io_stream[1];
+  cudaEvent_t* ev = h->io_ev;
+  // the copy streams start after the work already on the handle's stream
+  FDB_CUDA_TRY(cudaEventRecord(ev[0], cs));
+  FDB_CUDA_TRY(cudaStreamWaitEvent(up, ev[0], 0));
+  FDB_CUDA_TRY(cudaStreamWaitEvent(down, ev[0], 0));
+  FDB_CUDA_TRY(cudaMemcpyAsync(r.d[r.in], in[0], bytes, cudaMemcpyHostToDevice, up));
+  FDB_CUDA_TRY(cudaEventRecord(ev[1], up));
+  for (int k = 0; k < count; ++k) {
+    const int p = k & 1;
+    if (k + 1 < count) {
+      if (k >= 1) FDB_CUDA_TRY(cudaStreamWaitEvent(up, ev[5 + (p ^ 1)], 0));
+      FDB_CUDA_TRY(cudaMemcpyAsync(r.d[r.third], in[k + 1], bytes, cudaMemcpyHostToDevice, up));
+      FDB_CUDA_TRY(cudaEventRecord(ev[1 + (p ^ 1)], up));
+    }
+    FDB_CUDA_TRY(cudaStreamWaitEvent(cs, ev[1 + p], 0));
+    h->buf[0] = r.d[r.in];
+    h->buf[1] = r.d[r.other];
+    h->cur = 0;
+    h->scale_slot = -1;  // a new field: the fixed path measures max|f| again
+    if (num_steps > 0) FDB_TRY(advance(h, num_steps, dt, arith));
+    const int res = h->cur == 0 ? r.in : r.other;
+    const int spare = h->cur == 0 ? r.other : r.in;
+    FDB_TRY(launch_sum(r.d[res], h->g.ntot, h->part, dsum + k, cs));
+    FDB_CUDA_TRY(cudaEventRecord(ev[3 + p], cs));
+    FDB_CUDA_TRY(cudaStreamWaitEvent(down, ev[3 + p], 0));
+    FDB_CUDA_TRY(cudaMemcpyAsync(out[k], r.d[res], bytes, cudaMemcpyDeviceToHost, down));
+    FDB_CUDA_TRY(cudaEventRecord(ev[5 + p], down));
+    r.in = r.third;  // uploaded while this field advected
+    r.other = spare;
+    r.third = res;   // free again once its download ends
   }
   return FDB_OK;
 }
@@ -280,6 +442,12 @@ int fdb_upwind_destroy(fdb_upwind* h) {
   if (h->dpart) cudaFree(h->dpart);
   if (h->scratch) cudaFree(h->scratch);
   if (h->hscal) cudaFreeHost(h->hscal);
+  if (h->extra) cudaFree(h->extra);
+  if (h->tscratch) cudaFree(h->tscratch);
+  for (cudaStream_t s : h->io_stream)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : h->io_ev)
+    if (e) cudaEventDestroy(e);
   if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return FDB_OK;
@@ -318,14 +486,8 @@ int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt) {
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
   if (num_steps == 0) return FDB_OK;
-  int arith = FDB_ARITH_EXACT;
-  if (h->g.ndims <= 3) {
-    arith = resolve_arith(h, coeffs3(h->g, dt));
-    if (arith < 0)
-      return fail(FDB_ERR_UNSUPPORTED,
-                  "FDB_ARITH_FIXED requested but the geometry/coefficients are outside its "
-                  "domain (see fdb_upwind_set_arith)");
-  }
+  int arith = 0;
+  FDB_TRY(pick_arith(h, dt, &arith));
   h->arith_used = arith;
   return advance(h, num_steps, dt, arith);
 }
@@ -339,6 +501,65 @@ int fdb_upwind_checksum(fdb_upwind* h, double* out) {
   FDB_TRY(sync(h));
   *out = h->hscal[0];
   return FDB_OK;
+}
+
+int fdb_upwind_advect_host_stream(fdb_upwind* h, int count, const double* const* in,
+                                  double* const* out, int num_steps, double dt,
+                                  double* checksums) {
+  NvtxScope nvtx_("fdb.advect_host_stream");
+  FDB_TRY(check_handle(h));
+  if (count < 0) return fail(FDB_ERR_INVALID, "count must be >= 0");
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
+  if (count == 0) return FDB_OK;
+  if (!in || !out) return fail(FDB_ERR_INVALID, "null field array");
+  for (int k = 0; k < count; ++k)
+    if (!in[k] || !out[k]) return fail(FDB_ERR_INVALID, "null host field");
+  int arith = h->arith_used;
+  if (num_steps > 0) FDB_TRY(pick_arith(h, dt, &arith));
+  FDB_TRY(ensure_host_stream(h));
+  double* dsum = nullptr;
+  FDB_TRY(dalloc(&dsum, (size_t)count));
+  FieldRing r{{h->buf[h->cur], h->buf[h->cur ^ 1], h->extra}, 0, 1, 2};
+  int rc = host_stream_enqueue(h, count, in, out, num_steps, dt, arith, dsum, r);
+  // drain the copy streams before the buffers change hands
+  cudaError_t e0 = cudaStreamSynchronize(h->io_stream[0]);
+  cudaError_t e1 = cudaStreamSynchronize(h->io_stream[1]);
+  if (rc == FDB_OK) {
+    h->buf[0] = r.d[r.third];  // the last result
+    h->buf[1] = r.d[r.other];
+    h->extra = r.d[r.in];
+    h->arith_used = arith;
+    rc = sync(h);
+    if (rc == FDB_OK && e0 != cudaSuccess) rc = cuda_fail(e0, "upload stream");
+    if (rc == FDB_OK && e1 != cudaSuccess) rc = cuda_fail(e1, "download stream");
+  } else {
+    cudaStreamSynchronize(h->stream);
+    h->buf[0] = r.d[0];
+    h->buf[1] = r.d[1];
+    h->extra = r.d[2];
+    h->scale_slot = -1;
+  }
+  h->cur = 0;
+  if (rc == FDB_OK && checksums) {
+    cudaError_t e = cudaMemcpy(checksums, dsum, (size_t)count * sizeof(double),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "checksum copy");
+  }
+  cudaFree(dsum);
+  return rc;
+}
+
+int fdb_upwind_advect_transposed(fdb_upwind* h, int num_steps, double dt, const double* in,
+                                 double* out, int is_device) {
+  NvtxScope nvtx_("fdb.advect_transposed");
+  FDB_TRY(check_handle(h));
+  if (h->g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "the transposed advect serves ndims <= 3");
+  if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
+  if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
+  if (!in || !out) return fail(FDB_ERR_INVALID, "null input or output");
+  FDB_TRY(transposed_run(h, num_steps, dt, in, out, is_device, nullptr));
+  return sync(h);
 }
 
 int fdb_upwind_std(fdb_upwind* h, double* out) {
@@ -457,63 +678,23 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   // Default: the fixed-point adjoint (forward and recompute on the integer
   // pipes).  EXACT/FMA requests, or coefficients outside the fixed kernel's
   // domain, use the FP64 adjoint with FP64 recompute.
-  const bool fixed = (h->arith == FDB_ARITH_AUTO || h->arith == FDB_ARITH_FIXED) &&
-                     fixed_supported(g, c, 1) == FDB_OK &&
-                     fixed_supported(g, c, h->depth) == FDB_OK;
-  const int arith = fixed ? FDB_ARITH_FIXED
-                          : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
+  const int arith = adjoint_arith(h, c);
+  const bool fixed = arith == FDB_ARITH_FIXED;
 
   if (!grad_v) {
-    // dL/df0 only: grad_f0 = (A^T)^S lambda_T.  A^T is the upwind step with
-    // every direction reversed and the same Courant numbers, so the forward
-    // kernels on the transposed geometry (with the coefficients of g) apply
-    // it: no checkpoints, no recompute, no contraction.  The field is
-    // advanced to f_T as in the full path.
-    cudaEvent_t t0, t1, t2;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
-    cudaEventCreate(&t2);
-    cudaEventRecord(t0, h->stream);
+    // dL/df0 only: grad_f0 = (A^T)^S lambda_T by the forward kernels on the
+    // transposed geometry (transposed_run): no checkpoints, no recompute, no
+    // contraction.  The field is advanced to f_T as in the full path.
+    ScopedEvent t0, t1, t2;
+    cudaEventRecord(t0.e, h->stream);
     FDB_TRY(advance(h, S, dt, arith));
-    cudaEventRecord(t1, h->stream);
-    if (!h->lam[0]) {
-      int rc = dalloc(&h->lam[0], g.ntot);
-      if (!rc) rc = dalloc(&h->lam[1], g.ntot);
-      if (rc) {
-        free_adjoint(h);
-        return rc;
-      }
-    }
-    FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[0], lambda_T, bytes,
-                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                 h->stream));
-    const Geom gT = transposed_geom(g);
-    double* lb[2] = {h->lam[0], h->lam[1]};
-    int lc = 0;
-    if (arith == FDB_ARITH_FIXED) {
-      FixedTuning t = h->tune;
-      t.depth = h->depth;
-      FDB_TRY(launch_advect_fixed_ex(gT, c, S, t, lb, &lc, h->scratch, h->scratch_bytes, nullptr,
-                                     h->stream));
-      h->scale_slot = -1;  // the scratch slots now describe lambda, not the field
-    } else {
-      for (int k = 0; k < S; ++k) {
-        FDB_TRY(launch_step_f64(gT, c, arith, lb[lc], lb[lc ^ 1], h->stream));
-        lc ^= 1;
-      }
-    }
-    cudaEventRecord(t2, h->stream);
-    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, lb[lc], bytes,
-                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                 h->stream));
+    cudaEventRecord(t1.e, h->stream);
+    FDB_TRY(transposed_run(h, S, dt, lambda_T, grad_f0, is_device, t2.e));
     const int rc = sync(h);
     float ms = 0.f;
     h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
-    if (cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess) h->adj_ms[0] = ms;
-    if (cudaEventElapsedTime(&ms, t1, t2) == cudaSuccess) h->adj_ms[2] = ms;
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    cudaEventDestroy(t2);
+    if (cudaEventElapsedTime(&ms, t0.e, t1.e) == cudaSuccess) h->adj_ms[0] = ms;
+    if (cudaEventElapsedTime(&ms, t1.e, t2.e) == cudaSuccess) h->adj_ms[2] = ms;
     cudaGetLastError();
     return rc;
   }

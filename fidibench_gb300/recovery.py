@@ -6,7 +6,8 @@ For each instance: f_true = a sphere indicator, data = advect(f_true); start
 from f0 = 0 and take `iters` steps f0 <- f0 - lr * dL/df0 on
 L = sum over instances of 0.5 ||advect(f0) - data||^2, the gradient coming
 from torch.autograd through BatchAdvect (forward: the batch's persistent
-advect; backward: fdb_batch_adjoint, all instances in every launch).  The
+advect; backward: the transposed problems, fdb_batch_advect_transposed, all
+instances in every launch: the velocity is fixed, so only dL/df0 is needed).  The
 loss is a sum of per-instance terms, so each instance's gradient is its own.
 With sum_j a_j <= 1 the step operator is a contraction in the 2-norm, so
 lr = 1 is a safe step.
@@ -58,7 +59,10 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
         data = batch_advect_fn(f_true, vel, shapes, steps, dts)
     f0 = torch.zeros_like(f_true, requires_grad=True)
     misfit0, fd_err = None, []
+    it_s = []  # wall time of each iteration (the first carries the one-time setup)
     for it in range(iters):
+        torch.cuda.synchronize(device)
+        t_it = time.perf_counter()
         out = batch_advect_fn(f0, vel, shapes, steps, dts)
         per = 0.5 * ((out - data) ** 2).view(count, cells).sum(dim=1)
         if it == 0:
@@ -81,6 +85,8 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
             fd_err = (torch.abs(fd - exact) / torch.clamp(torch.abs(exact), min=1e-300)).tolist()
         with torch.no_grad():
             f0 -= lr * f0.grad
+        torch.cuda.synchronize(device)
+        it_s.append(time.perf_counter() - t_it)
     with torch.no_grad():
         out = batch_advect_fn(f0, vel, shapes, steps, dts)
         misfit = (0.5 * ((out - data) ** 2).view(count, cells).sum(dim=1)).cpu().numpy()
@@ -94,7 +100,9 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
             "field_rel_err_median": float(np.median(field_err)),
             "grad_fd_rel_err_max": max(fd_err) if fd_err else None,
             "ms_per_gd_iteration": el / (count * iters) * 1e3,
-            "mode": "all instances per launch (batched advect and adjoint)"}
+            "ms_per_gd_iteration_steady": (float(np.median(it_s[1:])) if len(it_s) > 1
+                                           else it_s[0]) / count * 1e3,
+            "mode": "all instances per launch (batched advect, batched transposed advect)"}
 
 
 __all__ = ["recover", "instance_specs", "sphere_field"]

@@ -187,6 +187,43 @@ class Upwind:
         check(lib.fdb_upwind_get_field(self._h, _capi.dptr(out), is_dev))
         return out
 
+    def advect_host_stream(self, fields, numTimeSteps: int, deltaTime: float,
+                           out=None) -> np.ndarray:
+        """The driver's cycle (upwind/cxx/upwind.cxx:194-199: initial field,
+        advect, checksum) over a sequence of host fields, with the upload of
+        the next field and the download of the previous result overlapping
+        each advect.  ``fields`` and ``out`` hold host buffers of ntot FP64
+        values (numpy arrays or CPU torch tensors, pinned for the overlap);
+        ``out`` defaults to writing the results back into ``fields``.
+        Returns the checksum of every result; the handle is left at the last
+        result."""
+        fields = list(fields)
+        out = fields if out is None else list(out)
+        if len(out) != len(fields):
+            raise ValueError("out needs one buffer per field")
+        for a in fields + out:
+            if getattr(a, "is_cuda", False):
+                raise ValueError("advect_host_stream takes host buffers")
+            ok = (a.dtype == np.float64 if isinstance(a, np.ndarray)
+                  else str(a.dtype) == "torch.float64")
+            contiguous = (a.flags.c_contiguous if isinstance(a, np.ndarray)
+                          else a.is_contiguous())
+            if not ok or not contiguous:
+                raise ValueError("host fields must be contiguous float64")
+            n = a.size if isinstance(a, np.ndarray) else a.numel()
+            if n != self.ntot:
+                raise ValueError(f"field has {n} values, expected {self.ntot}")
+        for a in out:
+            if isinstance(a, np.ndarray) and not a.flags.writeable:
+                raise ValueError("output buffers must be writeable")
+        cnt = len(fields)
+        ins = (ctypes.c_void_p * max(cnt, 1))(*[_capi.dptr(a) for a in fields])
+        outs = (ctypes.c_void_p * max(cnt, 1))(*[_capi.dptr(a) for a in out])
+        sums = np.zeros(cnt, dtype=np.float64)
+        check(lib.fdb_upwind_advect_host_stream(self._h, cnt, ins, outs, int(numTimeSteps),
+                                                float(deltaTime), sums.ctypes.data))
+        return sums
+
     def field_ptr(self) -> int:
         p = ctypes.c_void_p()
         check(lib.fdb_upwind_field_ptr(self._h, ctypes.byref(p)))
@@ -229,6 +266,37 @@ class Upwind:
                                      gv.ctypes.data if velocity_grad else None,
                                      int(checkpoint_every), is_dev))
         return grad_f0, gv
+
+    def advect_transposed(self, numTimeSteps: int, deltaTime: float, values, out=None):
+        """(A^T)^numTimeSteps applied to ``values`` (numpy array or CUDA
+        float64 tensor) without touching the field: the grad_f0 of
+        adjoint(velocity_grad=False), for callers that already hold f_T.
+        ``out`` (same kind) may be ``values``."""
+        is_dev = 1 if getattr(values, "is_cuda", False) else 0
+        if is_dev:
+            import torch
+            if values.dtype != torch.float64 or not values.is_contiguous():
+                raise ValueError("values must be a contiguous float64 tensor")
+            n = values.numel()
+            _order_after_torch(values)
+            if out is None:
+                out = torch.empty(self.ntot, dtype=torch.float64, device=values.device)
+        else:
+            values = _as_f64(values).reshape(-1)
+            n = values.size
+            if out is None:
+                out = np.empty(self.ntot, dtype=np.float64)
+            elif (not isinstance(out, np.ndarray) or out.dtype != np.float64
+                  or not out.flags.c_contiguous or not out.flags.writeable):
+                raise ValueError("out must be a writeable contiguous float64 array")
+        if n != self.ntot:
+            raise ValueError(f"values have {n} entries, expected {self.ntot}")
+        out_n = out.numel() if is_dev else out.size
+        if out_n != self.ntot or getattr(out, "is_cuda", False) != bool(is_dev):
+            raise ValueError("out must match values in size and kind")
+        check(lib.fdb_upwind_advect_transposed(self._h, int(numTimeSteps), float(deltaTime),
+                                               _capi.dptr(values), _capi.dptr(out), is_dev))
+        return out
 
     def adjoint_timings(self) -> dict:
         """Device milliseconds of the last adjoint call, by phase."""

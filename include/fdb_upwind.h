@@ -90,6 +90,25 @@ int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt);
  * Deterministic fixed-order tree sum on the device; synchronises. */
 int fdb_upwind_checksum(fdb_upwind* h, double* out);
 
+/* The driver's cycle (upwind/cxx/upwind.cxx:194-199: construct with the
+ * initial field, advect(numTimeSteps, dt), print checksum()) over `count`
+ * independent initial fields held in HOST memory: field k is read from in[k]
+ * (ntot doubles), advected with the same kernels, launch blocking and
+ * arithmetic as fdb_upwind_advect, written back to out[k], and its checksum (as
+ * fdb_upwind_checksum) stored in checksums[k] (checksums may be NULL).
+ * The upload of field k+1 and the download of field k-1 run on two copy
+ * streams while field k advects, so with pinned host buffers (cudaHostAlloc /
+ * cudaHostRegister) the host link is hidden behind the kernels; pageable
+ * buffers give the same results without the overlap.  out[k] may be in[k]
+ * and several in[k] (or several out[k]: the last field written wins) may
+ * share a buffer, but out[k] must not overlap any other in[j].  Needs one
+ * more field-sized device buffer (allocated on first use, freed with the
+ * handle).  On return the handle's field is the last result; synchronises.
+ * FDB_ERR_NONFINITE when any field held NaN/Inf on the fixed-point path. */
+int fdb_upwind_advect_host_stream(fdb_upwind* h, int count, const double* const* in,
+                                  double* const* out, int num_steps, double dt,
+                                  double* checksums);
+
 /* Replaces std() -- upwind.cxx:95-103 (population standard deviation). */
 int fdb_upwind_std(fdb_upwind* h, double* out);
 
@@ -146,6 +165,17 @@ int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius,
 int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
                        const double* lambda_T, double* grad_f0, double* grad_v,
                        int checkpoint_every, int is_device);
+
+/* The transpose of advect() alone: out = (A^T)^num_steps in, by the forward
+ * kernels (the handle's arithmetic) on the problem with every upwind direction
+ * reversed -- the dL/df0 part of fdb_upwind_adjoint (bit-identical to its
+ * grad_v = NULL result) without advancing the field: the field, and what the
+ * next advect continues from, are untouched.  For callers that already hold
+ * f_T (a reverse-mode framework's backward pass).  ntot values each; device
+ * pointers when is_device = 1; in == out allowed.  ndims <= 3.  Synchronises;
+ * FDB_ERR_NONFINITE when `in` holds NaN/Inf on the fixed-point path. */
+int fdb_upwind_advect_transposed(fdb_upwind* h, int num_steps, double dt, const double* in,
+                                 double* out, int is_device);
 
 /* Device time (ms) of the last fdb_upwind_adjoint call, by phase: ms3[0] =
  * forward pass with checkpoints, ms3[1] = recompute of the segment states
@@ -216,6 +246,13 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt);
  * problems with every upwind direction reversed (as in fdb_upwind_adjoint). */
 int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const double* lambda_T,
                       double* grad_f0, double* grad_v, int checkpoint_every, int is_device);
+/* The transpose of fdb_batch_advect alone for every instance: out = (A^T)^S
+ * in (the persistent launch on the problems with every upwind direction
+ * reversed), the batch's fields untouched; bit-identical to the grad_f0 of
+ * fdb_batch_adjoint with grad_v = NULL.  in and out hold the instances one
+ * after another in the caller's order; in == out allowed. */
+int fdb_batch_advect_transposed(fdb_batch* b, int num_steps, const double* dt, const double* in,
+                                double* out, int is_device);
 /* checksum() of every instance (upwind.cxx:91-93) into out[count]; synchronises. */
 int fdb_batch_checksums(fdb_batch* b, double* out);
 /* Times the compiled (depth, shape, tile_z) choices on a copy of the fields

@@ -167,3 +167,69 @@ def test_f0_only_adjoint_is_the_transposed_problem(fdb, arith, v):
     assert np.array_equal(up.f, ax)
     assert float(ax @ y) == pytest.approx(float(x @ g_fast), rel=1e-11)
     up.close()
+
+
+@pytest.mark.parametrize("arith", ["auto", "fma", "exact"])
+def test_advect_transposed_leaves_the_field(fdb, port, arith):
+    """fdb_upwind_advect_transposed: bit-identical to the grad_f0 of the
+    dL/df0-only adjoint, the field and the next advect untouched, the
+    oracle's transposed step applied S times, and in == out allowed."""
+    n, L, v = (20, 28, 36), (1.0, 1.3, 0.8), (0.7, -0.5, 0.35)
+    steps, dt = 17, 0.4 / 45
+    rng = np.random.default_rng(13)
+    x = rng.standard_normal(int(np.prod(n)))
+    y = rng.standard_normal(x.size)
+    up = fdb.Upwind(v, L, n, arith=arith)
+    up.f = x
+    up.advect(5, dt)
+    f5 = up.f
+    aty = up.advect_transposed(steps, dt, y)
+    # the field is untouched and the next advect continues as without the call
+    assert np.array_equal(up.f, f5)
+    up.advect(6, dt)
+    cont = up.f
+    ref = fdb.Upwind(v, L, n, arith=arith)
+    ref.f = x
+    ref.advect(5, dt)
+    ref.advect(6, dt)
+    assert np.array_equal(cont, ref.f)
+    # the same numbers as the adjoint's dL/df0-only path
+    ref.f = x
+    g_fast, _ = ref.adjoint(steps, dt, y, velocity_grad=False)
+    assert np.array_equal(aty, g_fast)
+    ref.close()
+    # the oracle's transposed step, S times (FP64; the coefficient part is unused)
+    lam = y.copy()
+    for _ in range(steps):
+        lam, _ = port.adjoint_step(n, v, L, dt, x, lam)
+    assert rel_maxnorm(aty, lam) <= 1e-13
+    # device buffers, in place
+    import torch
+    t = torch.tensor(y, device="cuda")
+    up.advect_transposed(steps, dt, t, t)
+    assert np.array_equal(t.cpu().numpy(), aty)
+    up.close()
+
+
+def test_advect_transposed_rejects_bad_input(fdb):
+    from fidibench_gb300._capi import FdbError
+    n, v = (12, 13, 14), (0.5, -0.4, 0.3)
+    up = fdb.Upwind(v, (1.0,) * 3, n, arith="fixed")
+    y = np.ones(int(np.prod(n)))
+    with pytest.raises(ValueError):
+        up.advect_transposed(3, 0.01, y[:-1])
+    with pytest.raises(ValueError):
+        up.advect_transposed(3, 0.01, y, out=np.empty(y.size, dtype=np.float32))
+    bad = y.copy()
+    bad[5] = np.inf
+    with pytest.raises(FdbError) as e:
+        up.advect_transposed(3, 0.01, bad)
+    assert e.value.code == 6
+    # still usable; zero steps is the identity
+    assert np.array_equal(up.advect_transposed(0, 0.01, y), y)
+    g4 = fdb.Upwind((0.1, 0.2, 0.3, 0.4), (1.0,) * 4, (3, 4, 5, 6))
+    with pytest.raises(FdbError) as e:
+        g4.advect_transposed(2, 0.01, np.ones(360))
+    assert e.value.code == 4
+    g4.close()
+    up.close()
