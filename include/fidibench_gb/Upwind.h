@@ -10,7 +10,8 @@
 //   double checksum() const                                     upwind.cxx:91-93
 //   double std() const                                          upwind.cxx:95-103
 //   void   print() const                                        upwind.cxx:105-109
-// Additions: setInitialCondition(), getField(), setArith(), handle().
+// Additions: setInitialCondition(), getField(), setArith(), handle(),
+// adjoint(), advectTransposed(), advectHostStream().
 //
 // Differences, by design: the field lives on the GPU (copied to the host only
 // by print/saveVTK/getField); errors throw std::runtime_error carrying
@@ -117,8 +118,9 @@ class Upwind {
   // counterpart; fdb_upwind_adjoint): runs advect(numTimeSteps, deltaTime)
   // from the current field with a checkpoint every checkpointEvery steps
   // (0: about sqrt(numTimeSteps)), then the transposed steps.  Returns
-  // dL/df0; gradVelocity (nullable) receives dL/dv (NDIMS values).  The field
-  // ends at f_T, as after advect.
+  // dL/df0; gradVelocity (nullable) receives dL/dv (NDIMS values).  Without
+  // gradVelocity only dL/df0 is computed (the transposed problem alone, no
+  // checkpoints).  The field ends at f_T, as after advect.
   std::vector<double> adjoint(int numTimeSteps, double deltaTime,
                               const std::vector<double>& lambdaT,
                               std::vector<double>* gradVelocity = nullptr,
@@ -126,11 +128,38 @@ class Upwind {
     if (lambdaT.size() != ntot_) throw std::invalid_argument("adjoint: wrong lambdaT size");
     std::vector<double> g(ntot_);
     std::vector<double> gv(NDIMS, 0.0);
-    check(fdb_upwind_adjoint(h_, numTimeSteps, deltaTime, lambdaT.data(), g.data(), gv.data(),
-                             checkpointEvery, 0),
+    check(fdb_upwind_adjoint(h_, numTimeSteps, deltaTime, lambdaT.data(), g.data(),
+                             gradVelocity ? gv.data() : nullptr, checkpointEvery, 0),
           "fdb_upwind_adjoint");
     if (gradVelocity) *gradVelocity = gv;
     return g;
+  }
+
+  // The transpose of advect alone (fdb_upwind_advect_transposed): returns
+  // (A^T)^numTimeSteps lambda -- dL/df0 for a caller that already holds f_T
+  // -- without touching the field.
+  std::vector<double> advectTransposed(int numTimeSteps, double deltaTime,
+                                       const std::vector<double>& lambda) {
+    if (lambda.size() != ntot_) throw std::invalid_argument("advectTransposed: wrong size");
+    std::vector<double> out(ntot_);
+    check(fdb_upwind_advect_transposed(h_, numTimeSteps, deltaTime, lambda.data(), out.data(), 0),
+          "fdb_upwind_advect_transposed");
+    return out;
+  }
+
+  // The driver's cycle (set the field, advect, checksum) over many host
+  // fields (fdb_upwind_advect_host_stream): fields[k] (size() doubles each)
+  // is advected in place and its checksum returned; the next upload and the
+  // previous download overlap each advect when the buffers are pinned.  The
+  // handle's field ends at the last result.
+  std::vector<double> advectHostStream(const std::vector<double*>& fields, int numTimeSteps,
+                                       double deltaTime) {
+    std::vector<double> sums(fields.size());
+    std::vector<const double*> in(fields.begin(), fields.end());
+    check(fdb_upwind_advect_host_stream(h_, (int)fields.size(), in.data(), fields.data(),
+                                        numTimeSteps, deltaTime, sums.data()),
+          "fdb_upwind_advect_host_stream");
+    return sums;
   }
 
   void setArith(int arith, int temporalDepth = 0) {

@@ -76,3 +76,17 @@ def test_upwind_class_rejects_mismatched_lengths():
     from fidibench_gb300 import Upwind
     with pytest.raises(ValueError):
         Upwind([1.0, 1.0], [1.0], [4, 4])
+
+
+def test_cpp_facade_check_compiles(tmp_path):
+    """The C++ facade test program builds against the headers and the library
+    (it runs in the GPU suite)."""
+    import subprocess
+    src = os.path.join(ROOT, "tests", "cpp", "facade_check.cpp")
+    lib_dir = os.path.join(ROOT, "fidibench_gb300", "_lib")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                        src, "-o", str(tmp_path / "facade_check"), "-L", lib_dir,
+                        "-lfdb_upwind", "-Wl,-rpath," + lib_dir],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "warning" not in r.stderr

@@ -125,3 +125,17 @@ def test_driver_adjoint_matches_python(fdb):
     up.close()
     assert np.allclose(gv, gv_ref, rtol=1e-12, atol=0.0)
     assert g_norm == pytest.approx(float(np.linalg.norm(g0)), rel=1e-12)
+
+
+def test_cpp_facade_additions(tmp_path):
+    """tests/cpp/facade_check.cpp: advectHostStream against the serial cycle
+    and advectTransposed against the dL/df0-only adjoint, bit for bit."""
+    src = os.path.join(ROOT, "tests", "cpp", "facade_check.cpp")
+    lib_dir = os.path.join(ROOT, "fidibench_gb300", "_lib")
+    exe = str(tmp_path / "facade_check")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o",
+                    exe, "-L", lib_dir, "-lfdb_upwind", "-Wl,-rpath," + lib_dir], check=True,
+                   timeout=300)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "facade ok" in r.stdout
