@@ -284,12 +284,12 @@ def gaussian_random_field(n: int, corr_cells: float, seed: int, device):
 
 def bench_adjoint(stream) -> dict:
     """Adjoint form: 256^3, v = (0.8, 0.5, -0.6), dt = 0.5 min dx/|v|, 200
-    steps, checkpoints every 20; L = 0.5 ||f_T - target||^2 with a seeded
-    Gaussian random field target (correlation length 8 cells).  Reports the
-    adjoint/forward per-step cost (with dL/dv, and for dL/df0 alone, which
-    is the transposed problem advected without checkpoints), the dot-product
-    test and central finite differences (h = 1e-6) on 16 seeded directions
-    and the 3 velocities."""
+    steps; L = 0.5 ||f_T - target||^2 with a seeded Gaussian random field
+    target (correlation length 8 cells).  Reports the adjoint/forward per-step
+    cost of the default form (dL/dv in closed form), of the step-by-step form
+    (checkpoints every 20 steps, recompute, a contraction per step) and of
+    dL/df0 alone; the dot-product test and central finite differences
+    (h = 1e-6) on 16 seeded directions and the 3 velocities (default form)."""
     import torch
     import fidibench_gb300 as fdb
 
@@ -333,6 +333,17 @@ def bench_adjoint(stream) -> dict:
         g0, gv = up.adjoint(ADJ_STEPS, dt, lam, checkpoint_every=ADJ_CKPT)
         timings.append(up.adjoint_timings())
     t = timings[-1]
+    # the step-by-step form (checkpoints every ADJ_CKPT steps, recompute, one
+    # contraction per transposed step) for comparison
+    up.set_adjoint_form("stepwise")
+    for _ in range(2):
+        up.set_field(f0)
+        g0_sw, gv_sw = up.adjoint(ADJ_STEPS, dt, lam, checkpoint_every=ADJ_CKPT)
+        t_sw = up.adjoint_timings()
+    up.set_adjoint_form("closed")
+    sw_gv_rel = float(np.max(np.abs(np.asarray(gv) - np.asarray(gv_sw))) /
+                      np.max(np.abs(np.asarray(gv_sw))))
+    sw_g0_rel = float(torch.max(torch.abs(g0_sw - g0)) / torch.max(torch.abs(g0_sw)))
     # dL/df0 alone: the transposed problem (every upwind direction reversed)
     for _ in range(2):
         up.set_field(f0)
@@ -373,13 +384,25 @@ def bench_adjoint(stream) -> dict:
     up.close()
     adj_step = t["adjoint_ms"] / ADJ_STEPS
     rec_step = t["recompute_ms"] / ADJ_STEPS
+    sw_adj = t_sw["adjoint_ms"] / ADJ_STEPS
+    sw_rec = t_sw["recompute_ms"] / ADJ_STEPS
     a_sum = sum(abs(v) * dt * ADJ_N for v in ADJ_V)
     return {"workload": "adjoint_256cube_200steps_ckpt20", "dt": dt,
             "courant_sum": a_sum, "forward_ms_per_step": fwd_ms_step,
+            "form": "closed: dL/da_j = S <lam^1, D_j f0>, lam^1 = (A^T)^(S-1) lam_T",
             "adjoint_ms_per_step": adj_step, "recompute_ms_per_step": rec_step,
             "adjoint_over_forward": adj_step / fwd_ms_step,
             "backward_incl_recompute_over_forward": (adj_step + rec_step) / fwd_ms_step,
+            "call_over_forward": (t["forward_ms"] + t["recompute_ms"] + t["adjoint_ms"]) /
+            ADJ_STEPS / fwd_ms_step,
             "adjoint_gcups": ADJ_N ** 3 / (adj_step * 1e-3) / 1e9,
+            "stepwise": {"adjoint_ms_per_step": sw_adj, "recompute_ms_per_step": sw_rec,
+                         "adjoint_over_forward": sw_adj / fwd_ms_step,
+                         "backward_incl_recompute_over_forward": (sw_adj + sw_rec) / fwd_ms_step,
+                         "call_over_forward": (t_sw["forward_ms"] + t_sw["recompute_ms"] +
+                                               t_sw["adjoint_ms"]) / ADJ_STEPS / fwd_ms_step,
+                         "grad_v_rel_diff_vs_closed": sw_gv_rel,
+                         "grad_f0_rel_diff_vs_closed": sw_g0_rel},
             "f0_only_ms_per_step": t_fast["adjoint_ms"] / ADJ_STEPS,
             "f0_only_over_forward": t_fast["adjoint_ms"] / ADJ_STEPS / fwd_ms_step,
             "f0_only_vs_full_rel_maxnorm": fast_vs_full,

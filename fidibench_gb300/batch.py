@@ -14,6 +14,9 @@ import numpy as np
 from . import _capi
 from ._capi import check, lib
 
+# how adjoint() computes dL/dv (FDB_TUNE_ADJOINT)
+_ADJOINT_FORMS = {"closed": 0, "stepwise": 1}
+
 
 class InstanceDesc(ctypes.Structure):
     _fields_ = [("ndims", ctypes.c_int), ("num_cells", ctypes.c_uint64 * 3),
@@ -83,13 +86,12 @@ class Batch:
                 velocity_grad: bool = True):
         """Gradients of a loss L(f_T of every instance) given lambda_T =
         dL/df_T: the instances' fields one after another (instance i starts
-        at sum(sizes[:i])), a numpy array or a CUDA float64 tensor.  Runs the
-        forward steps from the current fields (which end at f_T) and the
-        transposed steps backward for all instances at once.  Returns
-        (grad_f0 in the same concatenated form and kind, grad_v of shape
-        (count, 3): dL/dv per axis, 0 for missing axes).  velocity_grad=False
-        returns (grad_f0, None) from the transposed problems alone (every
-        upwind direction reversed): no checkpoints or recompute."""
+        at sum(sizes[:i])), a numpy array or a CUDA float64 tensor.  All
+        instances at once; the fields end at f_T.  Returns (grad_f0 in the
+        same concatenated form and kind, grad_v of shape (count, 3): dL/dv per
+        axis, 0 for missing axes).  dL/dv in closed form by default, or step
+        by step (set_adjoint_form("stepwise")).  velocity_grad=False returns
+        (grad_f0, None) from the transposed problems alone."""
         d = self._dts(dt)
         total = sum(self.sizes)
         is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
@@ -219,12 +221,19 @@ class Batch:
 
     def set_tuning(self, depth: int | None = None, shape: int | None = None,
                    tile_z: int | None = None) -> None:
+        """Launch-shape knobs of the persistent launch (None leaves a knob)."""
         if depth is not None:
             check(lib.fdb_batch_set_tuning(self._h, 3, int(depth)))
         if shape is not None:
             check(lib.fdb_batch_set_tuning(self._h, 2, int(shape)))
         if tile_z is not None:
             check(lib.fdb_batch_set_tuning(self._h, 1, int(tile_z)))
+
+    def set_adjoint_form(self, form: str = "closed") -> None:
+        """How adjoint() computes dL/dv: "closed" (default; S <lam^1, D_j f0>,
+        one contraction) or "stepwise" (checkpoints, one contraction per
+        transposed step)."""
+        check(lib.fdb_batch_set_tuning(self._h, 4, _ADJOINT_FORMS[form]))
 
     def autotune(self, numTimeSteps: int, dt, cache_path: str | None = None) -> dict:
         d = self._dts(dt)

@@ -360,6 +360,9 @@ struct fdb_batch {
   // plans built while set step the transposed problem (every upwind
   // direction reversed, the coefficients unchanged): the dL/df0-only adjoint
   bool transposed_run = false;
+  // adjoint form (FDB_TUNE_ADJOINT): 0 = dL/dv in closed form, 1 = step by step
+  int adj_mode = 0;
+  DeviceScratch contract;  // the closed form's contraction tables and partials
   std::vector<int64_t> offsets;  // cells
   std::vector<uint64_t> sizes;
   int64_t total = 0;
@@ -760,6 +763,7 @@ int fdb_batch_destroy(fdb_batch* b) {
   for (void* p : ps)
     if (p) cudaFree(p);
   free_batch_adjoint(b);
+  b->contract.release();
   if (b->h_sums) cudaFreeHost(b->h_sums);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
@@ -871,6 +875,10 @@ int fdb_batch_set_tuning(fdb_batch* b, int key, int value) {
   } else if (key == FDB_TUNE_TILE_Z) {
     if (value < 0) return fail(FDB_ERR_INVALID, "tile_z must be >= 0");
     b->tz = value;
+  } else if (key == FDB_TUNE_ADJOINT) {
+    if (value < 0 || value > 1) return fail(FDB_ERR_INVALID, "adjoint form must be 0 or 1");
+    b->adj_mode = value;
+    return FDB_OK;
   } else {
     return fail(FDB_ERR_INVALID, "unknown tuning key");
   }
@@ -901,11 +909,15 @@ int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt) {
   return run_looped(b, num_steps, dt, b->K);
 }
 
-// out = (A^T)^S in for all instances at once: the persistent launch on the
-// adjoint buffers with every upwind direction reversed; the fields are
-// untouched.
-static int batch_transposed(fdb_batch* b, int S, const double* dt, const double* lambda_T,
-                            double* grad_f0, int is_device) {
+// The transposed problems run on the adjoint buffers adj_lam[0..1] (the
+// fields are untouched): each instance's upwind directions reversed, its
+// coefficients unchanged, in its storage order.
+//
+// adj_lam[0] = the caller's concatenated fields `in`, permuted into the
+// storage order; `pref` receives where each instance starts in the caller's
+// layout.
+static int batch_lam_load(fdb_batch* b, const double* in, int is_device,
+                          std::vector<uint64_t>& pref) {
   const int n = b->count;
   const size_t T = (size_t)b->total;
   int rc = FDB_OK;
@@ -916,15 +928,15 @@ static int batch_transposed(fdb_batch* b, int S, const double* dt, const double*
     free_batch_adjoint(b);
     return rc;
   }
-  std::vector<uint64_t> pref(n);
+  pref.assign(n, 0);
   uint64_t cells = 0;
   for (int i = 0; i < n; ++i) {
     pref[i] = cells;
     cells += b->sizes[i];
   }
-  const double* lt = lambda_T;
+  const double* lt = in;
   if (!is_device) {
-    FDB_CUDA_TRY(cudaMemcpyAsync(b->adj_user, lambda_T, cells * 8, cudaMemcpyHostToDevice,
+    FDB_CUDA_TRY(cudaMemcpyAsync(b->adj_user, in, cells * 8, cudaMemcpyHostToDevice,
                                  b->stream));
     lt = b->adj_user;
   }
@@ -936,20 +948,32 @@ static int batch_transposed(fdb_batch* b, int S, const double* dt, const double*
       FDB_CUDA_TRY(cudaMemcpyAsync(dst, lt + pref[i], b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
                                    b->stream));
   }
-  // the persistent launch on the adjoint buffers, transposed problem
+  return FDB_OK;
+}
+
+// S transposed steps of every instance: the persistent launch on the adjoint
+// buffers; *lc (in/out) names the buffer that holds the state.
+static int batch_lam_steps(fdb_batch* b, int S, const double* dt, int* lc) {
+  if (S <= 0) return FDB_OK;
   const int cur = b->cur;
   std::swap(b->arena[0], b->adj_lam[0]);
   std::swap(b->arena[1], b->adj_lam[1]);
-  b->cur = 0;
+  b->cur = *lc;
   b->transposed_run = true;
-  rc = S > 0 ? run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, false) : FDB_OK;
-  const int lc = b->cur;
+  const int rc = run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, false);
+  *lc = b->cur;
   std::swap(b->arena[0], b->adj_lam[0]);
   std::swap(b->arena[1], b->adj_lam[1]);
   b->cur = cur;
   b->transposed_run = false;
-  if (rc) return rc;
-  double* gd = is_device ? grad_f0 : b->adj_user;
+  return rc;
+}
+
+// adj_lam[lc] back to the caller's order into `out`.
+static int batch_lam_store(fdb_batch* b, int lc, double* out, int is_device,
+                           const std::vector<uint64_t>& pref) {
+  const int n = b->count;
+  double* gd = is_device ? out : b->adj_user;
   for (int i = 0; i < n; ++i) {
     const double* src = b->adj_lam[lc] + b->offsets[i];
     if (b->permuted[i])
@@ -958,10 +982,67 @@ static int batch_transposed(fdb_batch* b, int S, const double* dt, const double*
       FDB_CUDA_TRY(cudaMemcpyAsync(gd + pref[i], src, b->sizes[i] * 8, cudaMemcpyDeviceToDevice,
                                    b->stream));
   }
-  if (!is_device)
-    FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, b->adj_user, cells * 8, cudaMemcpyDeviceToHost,
+  if (!is_device) {
+    const uint64_t cells = n ? pref[n - 1] + b->sizes[n - 1] : 0;
+    FDB_CUDA_TRY(cudaMemcpyAsync(out, b->adj_user, cells * 8, cudaMemcpyDeviceToHost,
                                  b->stream));
+  }
+  return FDB_OK;
+}
+
+// out = (A^T)^S in for all instances at once; the fields are untouched.
+static int batch_transposed(fdb_batch* b, int S, const double* dt, const double* lambda_T,
+                            double* grad_f0, int is_device) {
+  std::vector<uint64_t> pref;
+  FDB_TRY(batch_lam_load(b, lambda_T, is_device, pref));
+  int lc = 0;
+  FDB_TRY(batch_lam_steps(b, S, dt, &lc));
+  FDB_TRY(batch_lam_store(b, lc, grad_f0, is_device, pref));
   return bsync(b);
+}
+
+// dL/dv of every instance from dL/da of its stored axes: stored axis k is
+// view axis order[k], i.e. reference axis jj[order[k]];
+// a_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j (-dt up_j / dx_j).
+static void batch_velocity_grad(fdb_batch* b, const double* dt, const double* dda,
+                                double* grad_v) {
+  for (int i = 0; i < b->count; ++i) {
+    const Geom& gr = b->geoms_ref[i];
+    const int jj[3] = {gr.jz, gr.jy, gr.jx};
+    for (int k = 0; k < 3; ++k) grad_v[3 * i + k] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const int j = jj[b->order[i][k]];
+      if (j >= 0) grad_v[3 * i + j] = dda[3 * i + k] * (-dt[i] * (double)gr.up[j] / gr.dx[j]);
+    }
+  }
+}
+
+// The full gradient in closed form for every instance (the single-field
+// derivation: A, A^T and every D_j commute on the periodic grid, so
+// dL/da_j = S <lam^1, D_j f0> with lam^1 = (A^T)^(S-1) lam_T): S - 1
+// transposed steps, one contraction per instance with its field (still f0),
+// the last transposed step, then the forward advect to f_T.
+static int batch_adjoint_closed_form(fdb_batch* b, int S, const double* dt,
+                                     const double* lambda_T, double* grad_f0, double* grad_v,
+                                     int is_device) {
+  const int n = b->count;
+  if (!b->adj_dda) FDB_TRY(balloc(&b->adj_dda, 3 * (size_t)n));
+  std::vector<uint64_t> pref;
+  FDB_TRY(batch_lam_load(b, lambda_T, is_device, pref));
+  int lc = 0;
+  FDB_TRY(batch_lam_steps(b, S - 1, dt, &lc));
+  FDB_TRY(launch_vel_contract(n, b->geoms.data(), b->offsets.data(), b->arena[b->cur],
+                              b->adj_lam[lc], b->adj_dda, b->contract, b->stream));
+  FDB_TRY(batch_lam_steps(b, 1, dt, &lc));
+  FDB_TRY(batch_lam_store(b, lc, grad_f0, is_device, pref));
+  FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
+  std::vector<double> dda(3 * (size_t)n);
+  FDB_CUDA_TRY(cudaMemcpyAsync(dda.data(), b->adj_dda, dda.size() * 8, cudaMemcpyDeviceToHost,
+                               b->stream));
+  FDB_TRY(bsync(b));
+  for (double& x : dda) x *= (double)S;
+  batch_velocity_grad(b, dt, dda.data(), grad_v);
+  return FDB_OK;
 }
 
 // dL/df0 only (fdb_batch_adjoint with grad_v = NULL): the batch advances to
@@ -1005,6 +1086,19 @@ int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const doubl
         fixed_supported(b->geoms[i], cs[i], effective_K(b)) != FDB_OK)
       return fail(FDB_ERR_UNSUPPORTED, "batched adjoint: instance " + std::to_string(i) +
                                            " is outside the fixed-point kernel's domain");
+  }
+  if (b->adj_mode == 0) {
+    if (S == 0) {  // dL/df0 = lambda_T, dL/dv = 0
+      uint64_t cells = 0;
+      for (uint64_t z : b->sizes) cells += z;
+      FDB_TRY(bsync(b));
+      FDB_CUDA_TRY(cudaMemcpy(grad_f0, lambda_T, cells * 8,
+                              is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToHost));
+      for (int i = 0; i < 3 * n; ++i) grad_v[i] = 0.0;
+      return FDB_OK;
+    }
+    NvtxScope nvtx_c("fdb.batch.adjoint.closed_form");
+    return batch_adjoint_closed_form(b, S, dt, lambda_T, grad_f0, grad_v, is_device);
   }
   // storage
   const size_t T = (size_t)b->total;
@@ -1104,19 +1198,7 @@ int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const doubl
   FDB_CUDA_TRY(cudaMemcpyAsync(dda.data(), b->adj_dda, dda.size() * 8, cudaMemcpyDeviceToHost,
                                b->stream));
   FDB_TRY(bsync(b));
-  if (grad_v) {
-    // stored axis k is view axis order[k], i.e. reference axis jj[order[k]];
-    // a_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j (-dt up_j / dx_j)
-    for (int i = 0; i < n; ++i) {
-      const Geom& gr = b->geoms_ref[i];
-      const int jj[3] = {gr.jz, gr.jy, gr.jx};
-      for (int k = 0; k < 3; ++k) grad_v[3 * i + k] = 0.0;
-      for (int k = 0; k < 3; ++k) {
-        const int j = jj[b->order[i][k]];
-        if (j >= 0) grad_v[3 * i + j] = dda[3 * i + k] * (-dt[i] * (double)gr.up[j] / gr.dx[j]);
-      }
-    }
-  }
+  if (grad_v) batch_velocity_grad(b, dt, dda.data(), grad_v);
   return FDB_OK;
 }
 

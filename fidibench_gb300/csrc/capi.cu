@@ -51,6 +51,9 @@ struct fdb_upwind {
   // the transposed problem's own max|f| slots and error word, so that a
   // transposed run leaves the field's scale slot valid
   double* tscratch = nullptr;
+  // adjoint form: 0 = dL/dv in closed form, 1 = step by step with checkpoints
+  int adj_mode = 0;
+  fdb::DeviceScratch contract;  // the closed form's contraction tables and partials
   cudaStream_t io_stream[2] = {nullptr, nullptr};
   cudaEvent_t io_ev[7] = {};
 };
@@ -270,17 +273,15 @@ int adjoint_arith(fdb_upwind* h, const Coeffs3& c) {
                : ((h->arith == FDB_ARITH_EXACT) ? FDB_ARITH_EXACT : FDB_ARITH_FMA);
 }
 
-// out = (A^T)^S in.  A^T is the upwind step with every direction reversed and
-// the same Courant numbers, so the forward kernels on the transposed geometry
-// (with the coefficients of g) apply it.  Runs through the handle's adjoint
-// buffers with its own scale scratch: the field, its buffers and its scale
-// slot are untouched.  t_done (nullable) is recorded after the last step.
-int transposed_run(fdb_upwind* h, int S, double dt, const double* in, double* out,
-                   int is_device, cudaEvent_t t_done) {
+// The transposed problem runs through the handle's adjoint buffers lam[0..1]
+// with its own scale scratch, so the field, its buffers and its scale slot are
+// untouched.  A^T is the upwind step with every direction reversed and the
+// same Courant numbers, so the forward kernels on the transposed geometry
+// (with the coefficients of g) apply it.
+//
+// lam[0] = in (allocating the buffers on first use).
+int transposed_load(fdb_upwind* h, const double* in, int is_device) {
   const Geom& g = h->g;
-  const size_t bytes = g.ntot * sizeof(double);
-  const Coeffs3 c = coeffs3(g, dt);
-  const int arith = adjoint_arith(h, c);
   if (!h->lam[0]) {
     int rc = dalloc(&h->lam[0], g.ntot);
     if (!rc) rc = dalloc(&h->lam[1], g.ntot);
@@ -293,28 +294,96 @@ int transposed_run(fdb_upwind* h, int S, double dt, const double* in, double* ou
     FDB_TRY(dalloc(&h->tscratch, (fixed_scratch_bytes() + 7) / 8));
     FDB_CUDA_TRY(cudaMemsetAsync(h->tscratch, 0, h->scratch_bytes, h->stream));
   }
-  FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[0], in, bytes,
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->lam[0], in, g.ntot * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                h->stream));
-  const Geom gT = transposed_geom(g);
-  double* lb[2] = {h->lam[0], h->lam[1]};
-  int lc = 0;
+  return FDB_OK;
+}
+
+// Advance the adjoint buffers by S transposed steps: *lc (in/out) names the
+// buffer that holds the state, *slot (in/out, fixed path; -1: unknown) the
+// transposed scratch slot that describes it.  The state is FP64 on return.
+int transposed_steps(fdb_upwind* h, int S, double dt, int arith, int* lc, int* slot) {
+  if (S <= 0) return FDB_OK;
+  const Geom gT = transposed_geom(h->g);
+  const Coeffs3 c = coeffs3(h->g, dt);
   if (arith == FDB_ARITH_FIXED) {
     FixedTuning t = h->tune;
     t.depth = h->depth;
-    FDB_TRY(launch_advect_fixed_ex(gT, c, S, t, lb, &lc, h->tscratch, h->scratch_bytes, nullptr,
-                                   h->stream));
-  } else {
-    for (int k = 0; k < S; ++k) {
-      FDB_TRY(launch_step_f64(gT, c, arith, lb[lc], lb[lc ^ 1], h->stream));
-      lc ^= 1;
-    }
+    return launch_advect_fixed_ex(gT, c, S, t, h->lam, lc, h->tscratch, h->scratch_bytes, slot,
+                                  h->stream);
   }
+  *slot = -1;
+  for (int k = 0; k < S; ++k) {
+    FDB_TRY(launch_step_f64(gT, c, arith, h->lam[*lc], h->lam[*lc ^ 1], h->stream));
+    *lc ^= 1;
+  }
+  return FDB_OK;
+}
+
+// out = (A^T)^S in.  t_done (nullable) is recorded after the last step.
+int transposed_run(fdb_upwind* h, int S, double dt, const double* in, double* out,
+                   int is_device, cudaEvent_t t_done) {
+  const int arith = adjoint_arith(h, coeffs3(h->g, dt));
+  FDB_TRY(transposed_load(h, in, is_device));
+  int lc = 0, slot = -1;
+  FDB_TRY(transposed_steps(h, S, dt, arith, &lc, &slot));
   if (t_done) FDB_CUDA_TRY(cudaEventRecord(t_done, h->stream));
-  FDB_CUDA_TRY(cudaMemcpyAsync(out, lb[lc], bytes,
+  FDB_CUDA_TRY(cudaMemcpyAsync(out, h->lam[lc], h->g.ntot * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                h->stream));
   return FDB_OK;
+}
+
+// The full gradient in closed form.  The step is A = I + sum_j a_j D_j with
+// D_j = S_j - I, S_j the periodic shift by up_j along axis j: constant
+// coefficients on a periodic grid, so A, A^T and every D_j commute, and
+//   dL/da_j = sum_n <lam^{n+1}, D_j f^n>
+//           = sum_n <lam_T, A^{S-1-n} D_j A^n f0> = S <lam^1, D_j f0>,
+// lam^1 = (A^T)^{S-1} lam_T.  So: S - 1 transposed steps, one contraction with
+// the field (still f0), the last transposed step (dL/df0 = (A^T)^S lam_T),
+// then advect(S) leaves the field at f_T exactly as advect() does.  No
+// checkpoints and no recompute; the identity is exact for the discrete
+// scheme, so it agrees with the step-by-step form to rounding.
+int adjoint_closed_form(fdb_upwind* h, int S, double dt, int arith, const double* lambda_T,
+                        double* grad_f0, int is_device, double dda[3]) {
+  ScopedEvent t0, t1, t2;
+  cudaEventRecord(t0.e, h->stream);
+  FDB_TRY(transposed_load(h, lambda_T, is_device));
+  int lc = 0, slot = -1;
+  FDB_TRY(transposed_steps(h, S - 1, dt, arith, &lc, &slot));
+  const int64_t zero = 0;
+  FDB_TRY(launch_vel_contract(1, &h->g, &zero, h->buf[h->cur], h->lam[lc], h->dscal, h->contract,
+                              h->stream));
+  // the last step measures max|lam^1| afresh, as the batched form does, so
+  // that dL/df0 is the same bit for bit in both
+  slot = -1;
+  FDB_TRY(transposed_steps(h, 1, dt, arith, &lc, &slot));
+  cudaEventRecord(t1.e, h->stream);
+  FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], h->g.ntot * sizeof(double),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(advance(h, S, dt, arith));
+  cudaEventRecord(t2.e, h->stream);
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  float ms = 0.f;
+  h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
+  if (cudaEventElapsedTime(&ms, t1.e, t2.e) == cudaSuccess) h->adj_ms[0] = ms;
+  if (cudaEventElapsedTime(&ms, t0.e, t1.e) == cudaSuccess) h->adj_ms[2] = ms;
+  cudaGetLastError();
+  for (int k = 0; k < 3; ++k) dda[k] = (double)S * h->hscal[k];
+  return FDB_OK;
+}
+
+// dL/dv from dL/da of the internal axes (z, y, x):
+// a_j = -c_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j * (-dt up_j / dx_j).
+void velocity_grad(const Geom& g, double dt, const double dda[3], double* grad_v) {
+  const int jj[3] = {g.jz, g.jy, g.jx};
+  for (int j = 0; j < g.ndims; ++j) grad_v[j] = 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (jj[k] >= 0) grad_v[jj[k]] = dda[k] * (-dt * (double)g.up[jj[k]] / g.dx[jj[k]]);
 }
 
 // Buffers and streams of fdb_upwind_advect_host_stream, created on first use.
@@ -444,6 +513,7 @@ int fdb_upwind_destroy(fdb_upwind* h) {
   if (h->hscal) cudaFreeHost(h->hscal);
   if (h->extra) cudaFree(h->extra);
   if (h->tscratch) cudaFree(h->tscratch);
+  h->contract.release();
   for (cudaStream_t s : h->io_stream)
     if (s) cudaStreamDestroy(s);
   for (cudaEvent_t e : h->io_ev)
@@ -612,6 +682,11 @@ int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value) {
     h->tune.shape = value;
     return FDB_OK;
   }
+  if (key == FDB_TUNE_ADJOINT) {
+    if (value < 0 || value > 1) return fail(FDB_ERR_INVALID, "adjoint form must be 0 or 1");
+    h->adj_mode = value;
+    return FDB_OK;
+  }
   return fail(FDB_ERR_INVALID, "unknown tuning key");
 }
 
@@ -699,6 +774,21 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     return rc;
   }
 
+  if (h->adj_mode == 0) {
+    double dda[3] = {0.0, 0.0, 0.0};
+    if (S == 0) {
+      FDB_TRY(sync(h));
+      FDB_CUDA_TRY(cudaMemcpy(grad_f0, lambda_T, bytes,
+                              is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToHost));
+      h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
+    } else {
+      NvtxScope nvtx_c("fdb.adjoint.closed_form");
+      FDB_TRY(adjoint_closed_form(h, S, dt, arith, lambda_T, grad_f0, is_device, dda));
+    }
+    velocity_grad(g, dt, dda, grad_v);
+    return FDB_OK;
+  }
+
   // storage: nseg checkpoints, the segment's states (FP64: K - 1 buffers;
   // fixed point: two int64 chain buffers and K int32 arrays), two adjoint
   // buffers
@@ -752,7 +842,6 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     cudaEventDestroy(fe1);
     cudaGetLastError();
   };
-  const int jj[3] = {g.jz, g.jy, g.jx};
   double dda[3] = {0.0, 0.0, 0.0};  // dL/da (internal axes z, y, x)
 
   if (fixed) {
@@ -856,12 +945,7 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     // the FP64 kernel accumulates dL/dc = -dL/da
     for (int k = 0; k < 3; ++k) dda[k] = -h->hscal[k];
   }
-  if (grad_v) {
-    // a_j = -c_j = -dt v_j up_j / dx_j  =>  dL/dv_j = dL/da_j * (-dt up_j / dx_j)
-    for (int j = 0; j < g.ndims; ++j) grad_v[j] = 0.0;
-    for (int k = 0; k < 3; ++k)
-      if (jj[k] >= 0) grad_v[jj[k]] = dda[k] * (-dt * (double)g.up[jj[k]] / g.dx[jj[k]]);
-  }
+  velocity_grad(g, dt, dda, grad_v);
   return FDB_OK;
 }
 

@@ -135,6 +135,22 @@ int launch_adjoint_step(const Geom& g, const Coeffs3& c, const double* f,
                         cudaStream_t s);
 int launch_adjoint_finish(const double* dpart, double* d_out3, cudaStream_t s);
 
+// Device memory that grows on demand and is freed by its owner.
+struct DeviceScratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t need);
+  void release();
+};
+
+// The velocity contraction of the closed-form adjoint (adjoint.cu): for each
+// instance i (geometry geoms[i], cells at offsets[i] of f and lam),
+// d_out[3 i + k] = sum_c lam[c] (f[c + up_k e_k] - f[c]) over the internal
+// axes k = z, y, x.  Deterministic; two launches.
+int launch_vel_contract(int count, const Geom* geoms, const int64_t* offsets, const double* f,
+                        const double* lam, double* d_out, DeviceScratch& scratch,
+                        cudaStream_t s);
+
 // Fixed-point adjoint of a whole advect (adjoint_fixed.cu).  The forward
 // checkpoints ckpt[0..nseg) (FP64, every K steps) must already exist.
 struct AdjointFixedIO {

@@ -96,6 +96,14 @@ class Upwind:
         shared memory), -1 = automatic (3)."""
         check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
 
+    def set_adjoint_form(self, form: str = "closed") -> None:
+        """How adjoint() computes dL/dv: "closed" (default: the step's
+        operators commute on the periodic grid, so dL/da_j = S <lam^1, D_j f0>
+        with lam^1 = (A^T)^(S-1) lam_T -- one contraction, no checkpoints) or
+        "stepwise" (checkpoint/recompute and one contraction per transposed
+        step; checkpoint_every applies)."""
+        check(lib.fdb_upwind_set_tuning(self._h, 4, {"closed": 0, "stepwise": 1}[form]))
+
     def set_velocity(self, velocity) -> None:
         """New velocity for the same grid (the upwind directions follow its sign)."""
         v = _as_f64(velocity)
@@ -241,12 +249,12 @@ class Upwind:
                 checkpoint_every: int = 0, velocity_grad: bool = True):
         """Gradient of a loss L(f_T) given lambda_T = dL/df_T.
 
-        Runs the forward steps from the current field (which ends at f_T) and
-        the transposed steps backward with checkpoint/recompute.  Returns
-        (grad_f0, grad_v).  lambda_T/grad_f0 may be numpy arrays or CUDA
-        tensors (both of the same kind).  velocity_grad=False returns
-        (grad_f0, None) from the transposed problem alone (every upwind
-        direction reversed): no checkpoints or recompute."""
+        Returns (grad_f0, grad_v) and leaves the field at f_T.  dL/df0 comes
+        from the transposed problem (every upwind direction reversed); dL/dv
+        in closed form by default, or step by step with checkpoint/recompute
+        (set_adjoint_form("stepwise"); checkpoint_every applies).
+        lambda_T/grad_f0 may be numpy arrays or CUDA tensors (both of the same
+        kind).  velocity_grad=False returns (grad_f0, None)."""
         is_dev = 1 if getattr(lambda_T, "is_cuda", False) else 0
         if is_dev:
             _order_after_torch(lambda_T)

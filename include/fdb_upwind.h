@@ -137,6 +137,15 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
 #define FDB_TUNE_TILE_Z 1
 #define FDB_TUNE_SHAPE 2
 #define FDB_TUNE_DEPTH 3 /* batches only: steps per time block (0 = auto, 2..4) */
+/* FDB_TUNE_ADJOINT (single fields and batches): how fdb_*_adjoint computes
+ * dL/dv.  0 (default) = in closed form: the step is A = I + sum_j a_j D_j
+ * with D_j a periodic shift minus the identity, so A, A^T and every D_j
+ * commute and dL/da_j = S <lam^1, D_j f0> with lam^1 = (A^T)^(S-1) lam_T:
+ * one transposed run, one contraction and the forward advect, no
+ * checkpoints.  1 = step by step with checkpoints and recompute
+ * (checkpoint_every applies), one contraction per transposed step.  Both
+ * compute the same gradient of the discrete scheme, to rounding. */
+#define FDB_TUNE_ADJOINT 4
 int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value);
 
 /* Number of cells, and the arithmetic the last advect actually used. */
@@ -151,16 +160,19 @@ int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius,
 
 /* ---------------------------------------------------------------------------
  * Adjoint (no reference counterpart; the transpose of advect()).
- * Runs advect(num_steps, dt) forward from the handle's current field f0,
- * storing a checkpoint every `checkpoint_every` steps (0 = sqrt(num_steps)),
- * then runs the transposed step backward from lambda_T = dL/df_T, recomputing
- * each segment from its checkpoint.  Writes grad_f0 = dL/df0 (ntot values)
- * and grad_v = dL/dv (ndims values, host memory).  The handle's field is left
- * at f_T (as after advect).  Pointers are device memory when is_device = 1.
- * With grad_v = NULL only dL/df0 = (A^T)^S lambda_T is computed, by the
- * forward kernels on the problem with every upwind direction reversed (the
- * transpose of the step): no checkpoints, recompute or contraction, about the
- * cost of an advect; it agrees with the full path to rounding (1e-13).
+ * Gradients of a loss L(f_T), f_T = advect(num_steps, dt) of the handle's
+ * current field f0, given lambda_T = dL/df_T: writes grad_f0 = dL/df0 (ntot
+ * values) and grad_v = dL/dv (ndims values, host memory), and leaves the
+ * field at f_T (as after advect).  Pointers are device memory when
+ * is_device = 1.  dL/df0 = (A^T)^S lambda_T is the forward kernels run on the
+ * problem with every upwind direction reversed (the transpose of the step).
+ * dL/dv, by default (FDB_TUNE_ADJOINT 0), in closed form: S <lam^1, D_j f0>
+ * with lam^1 = (A^T)^(S-1) lambda_T, one contraction -- the whole call costs
+ * about two advects.  With FDB_TUNE_ADJOINT 1 it is summed step by step: a
+ * forward pass storing a checkpoint every `checkpoint_every` steps
+ * (0 = sqrt(num_steps)), then the transposed steps backward, each segment
+ * recomputed from its checkpoint, one contraction per step.  With
+ * grad_v = NULL only dL/df0 is computed.  The forms agree to rounding.
  * ------------------------------------------------------------------------- */
 int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt,
                        const double* lambda_T, double* grad_f0, double* grad_v,
@@ -228,13 +240,16 @@ int fdb_batch_init_sphere(fdb_batch* b, int index, const double* center, double 
 int fdb_batch_set_stream(fdb_batch* b, void* cuda_stream);
 /* New velocity of one instance (ndims values); the field is kept. */
 int fdb_batch_set_velocity(fdb_batch* b, int index, const double* velocity);
-/* keys FDB_TUNE_DEPTH, FDB_TUNE_SHAPE (2, 3 or 4), FDB_TUNE_TILE_Z */
+/* keys FDB_TUNE_DEPTH, FDB_TUNE_SHAPE (2, 3 or 4), FDB_TUNE_TILE_Z, FDB_TUNE_ADJOINT */
 int fdb_batch_set_tuning(fdb_batch* b, int key, int value);
 int fdb_batch_advect(fdb_batch* b, int num_steps, const double* dt);
 int fdb_batch_advect_looped(fdb_batch* b, int num_steps, const double* dt);
 /* Batched adjoint: fdb_upwind_adjoint for every instance at once (the
- * fixed-point adjoint; FDB_ERR_UNSUPPORTED when an instance is outside the
- * fixed kernel's domain).  The forward pass with checkpoints runs the
+ * fixed-point kernels; FDB_ERR_UNSUPPORTED when an instance is outside the
+ * fixed kernel's domain).  By default (FDB_TUNE_ADJOINT 0) dL/dv is in
+ * closed form: the transposed persistent launch, one contraction launch over
+ * all instances, then the forward persistent launch.  Step by step
+ * (FDB_TUNE_ADJOINT 1): the forward pass with checkpoints runs the
  * persistent launch; every recompute and transposed step is one launch over
  * all instances.  lambda_T and grad_f0 hold the instances' fields one after
  * another in the caller's order (instance i starts at the sum of the sizes of

@@ -71,10 +71,12 @@ def _forward(fdb, v, L, n, f0, steps, dt, arith="fma"):
     return out
 
 
+@pytest.mark.parametrize("form", ["closed", "stepwise"])
 @pytest.mark.parametrize("arith", ["fma", "fixed"])
-def test_finite_differences(fdb, port, arith):
+def test_finite_differences(fdb, port, arith, form):
     """FP64 adjoint (arith fma) and the fixed-point adjoint (arith fixed, the
-    default) against central differences of the same forward arithmetic."""
+    default), dL/dv in closed form and step by step, against central
+    differences of the same forward arithmetic."""
     n, L = (32, 24, 40), (1.0, 1.0, 1.0)
     v = np.array([0.8, 0.5, -0.6])
     steps, dt = 60, 0.5 / 40
@@ -82,6 +84,7 @@ def test_finite_differences(fdb, port, arith):
     f0 = port.sphere_noise(n, L, (0.5, 0.5, 0.5), 0.25, 0.01, 1)
     target = rng.standard_normal(f0.size)
     up = fdb.Upwind(v, L, n, arith=arith)
+    up.set_adjoint_form(form)
     up.f = f0
     up.advect(steps, dt)
     lam = up.f - target
@@ -105,8 +108,9 @@ def test_finite_differences(fdb, port, arith):
         assert gv[j] == pytest.approx(fd, rel=FD_TOL)
 
 
+@pytest.mark.parametrize("form", ["closed", "stepwise"])
 @pytest.mark.parametrize("v", [(1.0, -0.7, 0.3), (-0.3, -0.9, 0.6), (0.5, 0.0, -0.5)])
-def test_fixed_adjoint_matches_fp64_adjoint(fdb, v):
+def test_fixed_adjoint_matches_fp64_adjoint(fdb, v, form):
     """The two adjoint arithmetics agree: dL/df0 to 1e-12 of max|grad|; the
     velocity gradients to 1e-8, since the fixed-point contraction reads each
     forward state in 2^29 units (2^-30 of the fixed-point range), an
@@ -119,6 +123,7 @@ def test_fixed_adjoint_matches_fp64_adjoint(fdb, v):
     out = {}
     for arith in ("fma", "fixed"):
         up = fdb.Upwind(v, L, n, arith=arith)
+        up.set_adjoint_form(form)
         up.f = x
         out[arith] = up.adjoint(steps, dt, lam, checkpoint_every=10)
         up.close()
@@ -233,3 +238,68 @@ def test_advect_transposed_rejects_bad_input(fdb):
     assert e.value.code == 4
     g4.close()
     up.close()
+
+
+@pytest.mark.parametrize("arith", ["fixed", "fma"])
+@pytest.mark.parametrize("n,v,cfl", [((20, 28, 36), (0.7, -0.5, 0.35), 0.4),
+                                     ((24, 20, 28), (1.0, 1.0, 1.0), 0.5),  # sum a = 1.5 > 1
+                                     ((18, 26, 30), (0.5, 0.0, -0.5), 0.45),
+                                     ((33, 90), (0.6, -0.8), 0.4),
+                                     ((300,), (-0.5,), 0.7)])
+def test_closed_form_matches_stepwise(fdb, arith, n, v, cfl):
+    """dL/da_j = S <lam^1, D_j f0>: the closed form against the step-by-step
+    sum over every step (with checkpoints).  dL/dv to 1e-8 (the fixed-point
+    step-by-step contraction reads each forward state in 2^29 units), dL/df0
+    to rounding, and the field left at f_T exactly as advect() leaves it."""
+    L = (1.0,) * len(n)
+    dt = cfl * min(Lj / nj / abs(vj) for Lj, nj, vj in zip(L, n, v) if vj != 0.0)
+    steps = 23
+    rng = np.random.default_rng(sum(n))
+    x = rng.standard_normal(int(np.prod(n)))
+    lam = rng.standard_normal(x.size)
+    res = {}
+    for form in ("closed", "stepwise"):
+        up = fdb.Upwind(v, L, n, arith=arith)
+        up.set_adjoint_form(form)
+        up.f = x
+        g0, gv = up.adjoint(steps, dt, lam, checkpoint_every=5)
+        res[form] = (g0, gv, up.f)
+        up.close()
+    ref = fdb.Upwind(v, L, n, arith=arith)
+    ref.f = x
+    ref.advect(steps, dt)
+    f_t = ref.f
+    ref.close()
+    g_c, gv_c, f_c = res["closed"]
+    g_s, gv_s, _ = res["stepwise"]
+    assert np.array_equal(f_c, f_t)
+    assert rel_maxnorm(g_c, g_s) <= 1e-13
+    tol = 1e-8 if arith == "fixed" else 1e-11
+    assert np.allclose(gv_c, gv_s, rtol=tol, atol=tol * np.abs(gv_s).max())
+
+
+def test_closed_form_step_counts(fdb):
+    """S = 0 (identity, zero velocity gradient) and S = 1 (lam^1 = lam_T)."""
+    n, L, v = (16, 18, 20), (1.0, 1.0, 1.0), (0.4, -0.3, 0.6)
+    rng = np.random.default_rng(21)
+    x = rng.standard_normal(int(np.prod(n)))
+    lam = rng.standard_normal(x.size)
+    up = fdb.Upwind(v, L, n)
+    up.f = x
+    g0, gv = up.adjoint(0, 0.01, lam)
+    assert np.array_equal(g0, lam) and np.all(gv == 0.0)
+    assert np.array_equal(up.f, x)
+    g1, gv1 = up.adjoint(1, 0.01, lam)
+    up.set_adjoint_form("stepwise")
+    up.f = x
+    g1s, gv1s = up.adjoint(1, 0.01, lam)
+    assert rel_maxnorm(g1, g1s) <= 1e-13
+    assert np.allclose(gv1, gv1s, rtol=1e-8, atol=1e-8 * np.abs(gv1s).max())
+    from fidibench_gb300._capi import FdbError
+    with pytest.raises(KeyError):
+        up.set_adjoint_form("other")
+    from fidibench_gb300._capi import check, lib
+    with pytest.raises(FdbError):
+        check(lib.fdb_upwind_set_tuning(up._h, 4, 2))
+    up.close()
+

@@ -49,9 +49,8 @@ def test_batch_adjoint_matches_single_field(fdb):
         # the transposed steps are integer arithmetic: identical whatever the
         # tiling or the stored axis order
         assert np.array_equal(g0[off[k]:off[k + 1]], g_ref), k
-        # dL/dv: both contract with the forward states in 2^29 units, the
-        # batch's recomputed one step per launch, the handle's several steps
-        # per launch at one scale, so they agree to that precision
+        # dL/dv: the same closed-form contraction, summed in the stored axis
+        # order (permuted for the first instance), so equal to rounding
         nd = len(s["n"])
         assert np.allclose(gv[k, :nd], gv_ref, rtol=1e-8, atol=1e-8 * np.abs(gv_ref).max()), k
         assert np.all(gv[k, nd:] == 0.0)
@@ -137,18 +136,24 @@ def test_batch_adjoint_velocity_finite_differences(fdb):
             assert gv[k, j] == pytest.approx(fd, rel=1e-6), (k, j)
 
 
+@pytest.mark.parametrize("form", ["closed", "stepwise"])
 @pytest.mark.parametrize("steps,ck", [(0, 0), (1, 0), (6, 1), (5, 9), (11, 4)])
-def test_batch_adjoint_step_and_checkpoint_counts(fdb, steps, ck):
+def test_batch_adjoint_step_and_checkpoint_counts(fdb, steps, ck, form):
+    """Batch against single field at equal depth (the closed form's
+    transposed runs are blocked like the forward), both adjoint forms."""
     specs = SPECS[1:4]
     rng = np.random.default_rng(35)
     dts = _dts(specs)
     f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in specs]
     lam = [rng.standard_normal(x.size) for x in f0]
     b = _batch(fdb, specs, f0)
+    b.set_tuning(depth=4)
+    b.set_adjoint_form(form)
     g0, gv = b.adjoint(steps, dts, np.concatenate(lam), checkpoint_every=ck)
     off = np.cumsum([0] + [x.size for x in f0])
     for k, s in enumerate(specs):
-        up = fdb.Upwind(s["v"], s["L"], s["n"])
+        up = fdb.Upwind(s["v"], s["L"], s["n"], depth=4)
+        up.set_adjoint_form(form)
         up.f = f0[k]
         g_ref, gv_ref = up.adjoint(steps, dts[k], lam[k], checkpoint_every=ck)
         assert np.array_equal(g0[off[k]:off[k + 1]], g_ref), k
@@ -246,3 +251,31 @@ def test_batch_advect_transposed(fdb):
     with pytest.raises(ValueError):
         b.advect_transposed(3, dts, lam[:-1])
     b.close()
+
+
+def test_batch_closed_form_matches_stepwise(fdb):
+    """The batched closed form (dL/da_j = S <lam^1, D_j f0> per instance)
+    against the batched step-by-step adjoint, on the uneven instances
+    (permuted storage included), and the fields left at f_T either way."""
+    rng = np.random.default_rng(39)
+    dts = _dts(SPECS)
+    f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in SPECS]
+    lam = np.concatenate([rng.standard_normal(x.size) for x in f0])
+    res = {}
+    for form in ("closed", "stepwise"):
+        b = _batch(fdb, SPECS, f0)
+        b.set_adjoint_form(form)
+        g0, gv = b.adjoint(21, dts, lam, checkpoint_every=6)
+        res[form] = (g0, gv, [b.get_field(k) for k in range(len(SPECS))])
+        b.close()
+    g_c, gv_c, f_c = res["closed"]
+    g_s, gv_s, f_s = res["stepwise"]
+    off = np.cumsum([0] + [x.size for x in f0])
+    for k, s in enumerate(SPECS):
+        assert rel_maxnorm(g_c[off[k]:off[k + 1]], g_s[off[k]:off[k + 1]]) <= 1e-13, k
+        nd = len(s["n"])
+        assert np.allclose(gv_c[k, :nd], gv_s[k, :nd], rtol=1e-8,
+                           atol=1e-8 * np.abs(gv_s[k]).max()), k
+        # the step-by-step forward runs segment by segment: f_T to rounding
+        assert rel_maxnorm(f_c[k], f_s[k]) <= 1e-13, k
+
