@@ -79,13 +79,19 @@ class UpwindAdvect(torch.autograd.Function):
             up.advect_transposed(num_steps, dt, lam, g0)
             return g0.view_as(f0), None, None, None, None, None
         up.set_field(f0)
+        # the closed form with the field kept at f0: the forward already
+        # produced f_T, so one transposed run and one contraction
+        up.set_adjoint_form("closed_keep" if ck == 0 else "stepwise")
         g0, gv = up.adjoint(num_steps, dt, lam, g0, checkpoint_every=ck)
         grad_v = torch.as_tensor(np.asarray(gv), dtype=velocity.dtype, device=velocity.device)
         return g0.view_as(f0), grad_v, None, None, None, None
 
 
 def advect_fn(f0, velocity, num_steps: int, dt: float, lengths=None, checkpoint_every: int = 0):
-    """Differentiable advect: returns f after num_steps steps of size dt."""
+    """Differentiable advect: returns f after num_steps steps of size dt.
+    The backward pass takes dL/dv in closed form (one transposed run and one
+    contraction); checkpoint_every > 0 asks for the step-by-step adjoint with
+    checkpoints at that spacing instead (the same gradient, to rounding)."""
     if lengths is None:
         lengths = (1.0,) * f0.dim()
     if not torch.is_tensor(velocity):
@@ -162,6 +168,7 @@ class BatchAdvect(torch.autograd.Function):
             g0 = b.advect_transposed(num_steps, dts, lam)
             return g0.view_as(grad_out), None, None, None, None, None, None
         b.set_fields(f0c)
+        b.set_adjoint_form("closed_keep" if ck == 0 else "stepwise")
         g0, gv = b.adjoint(num_steps, dts, lam, checkpoint_every=ck)
         grad_v = torch.as_tensor(gv, dtype=velocity.dtype, device=velocity.device)
         return g0.view_as(grad_out), grad_v, None, None, None, None, None
@@ -170,7 +177,8 @@ class BatchAdvect(torch.autograd.Function):
 def batch_advect_fn(f0, velocity, shapes, num_steps: int, dts, lengths=None,
                     checkpoint_every: int = 0):
     """Differentiable batched advect (see BatchAdvect): returns the
-    concatenated fields after num_steps steps."""
+    concatenated fields after num_steps steps; checkpoint_every as in
+    advect_fn."""
     if lengths is None:
         lengths = [(1.0,) * len(n) for n in shapes]
     shapes = [tuple(int(x) for x in n) for n in shapes]

@@ -15,7 +15,7 @@ from . import _capi
 from ._capi import check, lib
 
 # how adjoint() computes dL/dv (FDB_TUNE_ADJOINT)
-_ADJOINT_FORMS = {"closed": 0, "stepwise": 1}
+_ADJOINT_FORMS = {"closed": 0, "stepwise": 1, "closed_keep": 2}
 
 
 class InstanceDesc(ctypes.Structure):
@@ -231,8 +231,8 @@ class Batch:
 
     def set_adjoint_form(self, form: str = "closed") -> None:
         """How adjoint() computes dL/dv: "closed" (default; S <lam^1, D_j f0>,
-        one contraction) or "stepwise" (checkpoints, one contraction per
-        transposed step)."""
+        one contraction), "stepwise" (checkpoints, one contraction per
+        transposed step) or "closed_keep" (closed, the fields left at f0)."""
         check(lib.fdb_batch_set_tuning(self._h, 4, _ADJOINT_FORMS[form]))
 
     def autotune(self, numTimeSteps: int, dt, cache_path: str | None = None) -> dict:

@@ -1,8 +1,10 @@
 """Small stand-alone runs of one kernel family, for profiling a single launch
 on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
 
-  adjoint N S : N^3 field, v = (0.8, 0.5, -0.6), dt = 0.5 min(dx/|v|), three
-                adjoint calls of S steps with one checkpoint segment
+  adjoint N S [form] : N^3 field, v = (0.8, 0.5, -0.6), dt = 0.5 min(dx/|v|),
+                three adjoint calls of S steps; form "closed" (default: dL/dv
+                in closed form) or "stepwise" (one checkpoint segment, the
+                recompute and one contraction per transposed step)
   advect N S  : N^3 sphere + noise field, v = (1, -0.7, 0.3), dt = 0.5/N,
                 three advect calls of S steps
   batch C S   : C seeded instances with axes in [32, 160] (the benchmark's
@@ -17,12 +19,13 @@ from __future__ import annotations
 import sys
 
 
-def adjoint_case(n: int, steps: int) -> dict:
+def adjoint_case(n: int, steps: int, form: str = "closed") -> dict:
     import torch
     import fidibench_gb300 as fdb
     v = (0.8, 0.5, -0.6)
     dt = 0.5 * min(1.0 / n / abs(x) for x in v)
     up = fdb.Upwind(v, (1.0,) * 3, (n,) * 3)
+    up.set_adjoint_form(form)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(1)
     lam = torch.randn(n ** 3, device="cuda", dtype=torch.float64, generator=gen)
@@ -77,10 +80,10 @@ def filter_case(n: int, iters: int) -> float:
 def main(argv: list[str]) -> int:
     cases = {"adjoint": adjoint_case, "advect": advect_case, "batch": batch_case,
              "filter": filter_case}
-    if len(argv) != 3 or argv[0] not in cases:
+    if len(argv) < 3 or argv[0] not in cases or (len(argv) > 3 and argv[0] != "adjoint"):
         print(__doc__)
         return 2
-    print(cases[argv[0]](int(argv[1]), int(argv[2])))
+    print(cases[argv[0]](int(argv[1]), int(argv[2]), *argv[3:4]))
     return 0
 
 

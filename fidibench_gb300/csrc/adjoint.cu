@@ -156,17 +156,20 @@ k_vel_contract(const double* __restrict__ f, const double* __restrict__ lam,
   }
 }
 
-// out[3 i + k] = the sum of instance i's block partials of axis k, in block order
-__global__ void k_vel_contract_finish(const double* __restrict__ part,
-                                      const ContractDev* __restrict__ insts, int count,
-                                      double* __restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 3 * count) return;
-  const ContractDev I = insts[t / 3];
-  const int k = t - 3 * (t / 3);
+// out[3 i + k] = the sum of instance i's block partials of axis k: one CTA
+// per (instance, axis), each thread a fixed stride of the blocks, then the
+// fixed-order tree of block_sum
+__global__ void __launch_bounds__(kThreads)
+k_vel_contract_finish(const double* __restrict__ part, const ContractDev* __restrict__ insts,
+                      double* __restrict__ out) {
+  __shared__ double sh[kThreads];
+  const int i = blockIdx.x / 3;
+  const int k = blockIdx.x - 3 * i;
+  const ContractDev I = insts[i];
   double acc = 0.0;
-  for (int b = 0; b < I.nblocks; ++b) acc = acc + part[3 * (I.block0 + b) + k];
-  out[t] = acc;
+  for (int b = threadIdx.x; b < I.nblocks; b += kThreads) acc = acc + part[3 * (I.block0 + b) + k];
+  const double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = t;
 }
 
 }  // namespace
@@ -215,7 +218,7 @@ int launch_vel_contract(int count, const Geom* geoms, const int64_t* offsets, co
   FDB_CUDA_TRY(cudaMemcpyAsync(d_table, block_inst.data(), total * sizeof(int),
                                cudaMemcpyHostToDevice, s));
   k_vel_contract<<<total, kThreads, 0, s>>>(f, lam, d_insts, d_table, d_part);
-  k_vel_contract_finish<<<(3 * count + 127) / 128, 128, 0, s>>>(d_part, d_insts, count, d_out);
+  k_vel_contract_finish<<<3 * count, kThreads, 0, s>>>(d_part, d_insts, d_out);
   note_launch(2);
   FDB_CUDA_TRY(cudaGetLastError());
   return FDB_OK;

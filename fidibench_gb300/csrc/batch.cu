@@ -876,7 +876,7 @@ int fdb_batch_set_tuning(fdb_batch* b, int key, int value) {
     if (value < 0) return fail(FDB_ERR_INVALID, "tile_z must be >= 0");
     b->tz = value;
   } else if (key == FDB_TUNE_ADJOINT) {
-    if (value < 0 || value > 1) return fail(FDB_ERR_INVALID, "adjoint form must be 0 or 1");
+    if (value < 0 || value > 2) return fail(FDB_ERR_INVALID, "adjoint form must be 0, 1 or 2");
     b->adj_mode = value;
     return FDB_OK;
   } else {
@@ -1024,7 +1024,7 @@ static void batch_velocity_grad(fdb_batch* b, const double* dt, const double* dd
 // the last transposed step, then the forward advect to f_T.
 static int batch_adjoint_closed_form(fdb_batch* b, int S, const double* dt,
                                      const double* lambda_T, double* grad_f0, double* grad_v,
-                                     int is_device) {
+                                     int is_device, bool advance_fields) {
   const int n = b->count;
   if (!b->adj_dda) FDB_TRY(balloc(&b->adj_dda, 3 * (size_t)n));
   std::vector<uint64_t> pref;
@@ -1035,7 +1035,8 @@ static int batch_adjoint_closed_form(fdb_batch* b, int S, const double* dt,
                               b->adj_lam[lc], b->adj_dda, b->contract, b->stream));
   FDB_TRY(batch_lam_steps(b, 1, dt, &lc));
   FDB_TRY(batch_lam_store(b, lc, grad_f0, is_device, pref));
-  FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
+  if (advance_fields)
+    FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
   std::vector<double> dda(3 * (size_t)n);
   FDB_CUDA_TRY(cudaMemcpyAsync(dda.data(), b->adj_dda, dda.size() * 8, cudaMemcpyDeviceToHost,
                                b->stream));
@@ -1049,7 +1050,8 @@ static int batch_adjoint_closed_form(fdb_batch* b, int S, const double* dt,
 // f_T, then the transposed launch gives (A^T)^S lambda_T.
 static int batch_adjoint_f0_only(fdb_batch* b, int S, const double* dt, const double* lambda_T,
                                  double* grad_f0, int is_device) {
-  if (S > 0) FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
+  if (S > 0 && b->adj_mode != 2)  // form 2 keeps the fields at f0
+    FDB_TRY(run_batched(b, S, dt, effective_K(b), effective_shape(b), b->tz, true));
   return batch_transposed(b, S, dt, lambda_T, grad_f0, is_device);
 }
 
@@ -1087,7 +1089,7 @@ int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const doubl
       return fail(FDB_ERR_UNSUPPORTED, "batched adjoint: instance " + std::to_string(i) +
                                            " is outside the fixed-point kernel's domain");
   }
-  if (b->adj_mode == 0) {
+  if (b->adj_mode != 1) {
     if (S == 0) {  // dL/df0 = lambda_T, dL/dv = 0
       uint64_t cells = 0;
       for (uint64_t z : b->sizes) cells += z;
@@ -1098,7 +1100,8 @@ int fdb_batch_adjoint(fdb_batch* b, int num_steps, const double* dt, const doubl
       return FDB_OK;
     }
     NvtxScope nvtx_c("fdb.batch.adjoint.closed_form");
-    return batch_adjoint_closed_form(b, S, dt, lambda_T, grad_f0, grad_v, is_device);
+    return batch_adjoint_closed_form(b, S, dt, lambda_T, grad_f0, grad_v, is_device,
+                                     b->adj_mode == 0);
   }
   // storage
   const size_t T = (size_t)b->total;

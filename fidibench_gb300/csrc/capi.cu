@@ -346,7 +346,7 @@ int transposed_run(fdb_upwind* h, int S, double dt, const double* in, double* ou
 // checkpoints and no recompute; the identity is exact for the discrete
 // scheme, so it agrees with the step-by-step form to rounding.
 int adjoint_closed_form(fdb_upwind* h, int S, double dt, int arith, const double* lambda_T,
-                        double* grad_f0, int is_device, double dda[3]) {
+                        double* grad_f0, int is_device, bool advance_field, double dda[3]) {
   ScopedEvent t0, t1, t2;
   cudaEventRecord(t0.e, h->stream);
   FDB_TRY(transposed_load(h, lambda_T, is_device));
@@ -363,7 +363,7 @@ int adjoint_closed_form(fdb_upwind* h, int S, double dt, int arith, const double
   FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], h->g.ntot * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                h->stream));
-  FDB_TRY(advance(h, S, dt, arith));
+  if (advance_field) FDB_TRY(advance(h, S, dt, arith));
   cudaEventRecord(t2.e, h->stream);
   FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost,
                                h->stream));
@@ -683,7 +683,7 @@ int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value) {
     return FDB_OK;
   }
   if (key == FDB_TUNE_ADJOINT) {
-    if (value < 0 || value > 1) return fail(FDB_ERR_INVALID, "adjoint form must be 0 or 1");
+    if (value < 0 || value > 2) return fail(FDB_ERR_INVALID, "adjoint form must be 0, 1 or 2");
     h->adj_mode = value;
     return FDB_OK;
   }
@@ -759,10 +759,11 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
   if (!grad_v) {
     // dL/df0 only: grad_f0 = (A^T)^S lambda_T by the forward kernels on the
     // transposed geometry (transposed_run): no checkpoints, no recompute, no
-    // contraction.  The field is advanced to f_T as in the full path.
+    // contraction.  The field is advanced to f_T as in the full path (kept
+    // at f0 in form 2).
     ScopedEvent t0, t1, t2;
     cudaEventRecord(t0.e, h->stream);
-    FDB_TRY(advance(h, S, dt, arith));
+    if (h->adj_mode != 2) FDB_TRY(advance(h, S, dt, arith));
     cudaEventRecord(t1.e, h->stream);
     FDB_TRY(transposed_run(h, S, dt, lambda_T, grad_f0, is_device, t2.e));
     const int rc = sync(h);
@@ -774,7 +775,7 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     return rc;
   }
 
-  if (h->adj_mode == 0) {
+  if (h->adj_mode != 1) {
     double dda[3] = {0.0, 0.0, 0.0};
     if (S == 0) {
       FDB_TRY(sync(h));
@@ -783,7 +784,8 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
       h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
     } else {
       NvtxScope nvtx_c("fdb.adjoint.closed_form");
-      FDB_TRY(adjoint_closed_form(h, S, dt, arith, lambda_T, grad_f0, is_device, dda));
+      FDB_TRY(adjoint_closed_form(h, S, dt, arith, lambda_T, grad_f0, is_device,
+                                  h->adj_mode == 0, dda));
     }
     velocity_grad(g, dt, dda, grad_v);
     return FDB_OK;

@@ -101,8 +101,10 @@ class Upwind:
         operators commute on the periodic grid, so dL/da_j = S <lam^1, D_j f0>
         with lam^1 = (A^T)^(S-1) lam_T -- one contraction, no checkpoints) or
         "stepwise" (checkpoint/recompute and one contraction per transposed
-        step; checkpoint_every applies)."""
-        check(lib.fdb_upwind_set_tuning(self._h, 4, {"closed": 0, "stepwise": 1}[form]))
+        step; checkpoint_every applies) or "closed_keep" (the closed form
+        with the field left at f0, for callers that already hold f_T)."""
+        check(lib.fdb_upwind_set_tuning(self._h, 4,
+                                        {"closed": 0, "stepwise": 1, "closed_keep": 2}[form]))
 
     def set_velocity(self, velocity) -> None:
         """New velocity for the same grid (the upwind directions follow its sign)."""

@@ -143,8 +143,11 @@ int fdb_upwind_set_arith(fdb_upwind* h, int arith, int temporal_depth);
  * commute and dL/da_j = S <lam^1, D_j f0> with lam^1 = (A^T)^(S-1) lam_T:
  * one transposed run, one contraction and the forward advect, no
  * checkpoints.  1 = step by step with checkpoints and recompute
- * (checkpoint_every applies), one contraction per transposed step.  Both
- * compute the same gradient of the discrete scheme, to rounding. */
+ * (checkpoint_every applies), one contraction per transposed step.  2 = the
+ * closed form with the field(s) left at f0 instead of f_T, for callers that
+ * already hold f_T (a reverse-mode framework's backward pass): one transposed
+ * run and one contraction.  All compute the same gradient of the discrete
+ * scheme, to rounding. */
 #define FDB_TUNE_ADJOINT 4
 int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value);
 

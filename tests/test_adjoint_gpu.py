@@ -300,6 +300,37 @@ def test_closed_form_step_counts(fdb):
         up.set_adjoint_form("other")
     from fidibench_gb300._capi import check, lib
     with pytest.raises(FdbError):
-        check(lib.fdb_upwind_set_tuning(up._h, 4, 2))
+        check(lib.fdb_upwind_set_tuning(up._h, 4, 3))
     up.close()
+
+
+def test_closed_form_keeping_the_field(fdb):
+    """Form "closed_keep": the closed form's gradients bit for bit, with the
+    field left at f0 (single field and batch)."""
+    n, L, v = (18, 22, 26), (1.0, 1.0, 1.0), (0.6, -0.4, 0.3)
+    dt = 0.4 / 26
+    rng = np.random.default_rng(22)
+    x = rng.standard_normal(int(np.prod(n)))
+    lam = rng.standard_normal(x.size)
+    up = fdb.Upwind(v, L, n)
+    up.f = x
+    g_c, gv_c = up.adjoint(17, dt, lam)
+    up.set_adjoint_form("closed_keep")
+    up.f = x
+    g_k, gv_k = up.adjoint(17, dt, lam)
+    assert np.array_equal(g_k, g_c) and np.array_equal(gv_k, gv_c)
+    assert np.array_equal(up.f, x)
+    g_f, _ = up.adjoint(17, dt, lam, velocity_grad=False)
+    assert np.array_equal(up.f, x)
+    assert rel_maxnorm(g_f, g_c) <= 1e-13
+    up.close()
+    b = fdb.Batch([(v, L, n)])
+    b.set_field(0, x)
+    gb_c, gvb_c = b.adjoint(17, [dt], lam)
+    b.set_adjoint_form("closed_keep")
+    b.set_field(0, x)
+    gb_k, gvb_k = b.adjoint(17, [dt], lam)
+    assert np.array_equal(gb_k, gb_c) and np.array_equal(gvb_k, gvb_c)
+    assert np.array_equal(b.get_field(0), x)
+    b.close()
 
