@@ -193,9 +193,10 @@ int fdb_upwind_advect_transposed(fdb_upwind* h, int num_steps, double dt, const 
                                  double* out, int is_device);
 
 /* Device time (ms) of the last fdb_upwind_adjoint call, by phase: ms3[0] =
- * forward pass with checkpoints, ms3[1] = recompute of the segment states
- * (fixed-point path; 0 for the FP64 path, whose recompute is interleaved),
- * ms3[2] = transposed steps (in the FP64 path: recompute + transposed steps). */
+ * forward pass (with checkpoints in the step-by-step form), ms3[1] =
+ * recompute of the segment states (step-by-step fixed-point path only),
+ * ms3[2] = transposed steps (with the closed form's contraction; in the
+ * step-by-step FP64 path: recompute + transposed steps). */
 int fdb_upwind_adjoint_timings(fdb_upwind* h, double* ms3);
 
 /* One transposed step on caller buffers (device pointers):
