@@ -152,9 +152,10 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def cpu_sample(threads: int | None = None, time_steps: int = 2):
+def cpu_sample(threads: int | None = None, time_steps: int = 2, one_thread: bool = False):
     """Reference algorithm on the host: a bounded sample of the workload (the
-    full 512^3 field, `time_steps` time steps), all host threads."""
+    full 512^3 field, `time_steps` time steps), all host threads; with
+    one_thread also the restatement on a single core (one time step)."""
     from oracle import Port, Reference
     port = Port()
     f0 = port.sphere_noise(SHAPE, LENGTHS, CENTER, RADIUS, NOISE, SEED)
@@ -173,11 +174,18 @@ def cpu_sample(threads: int | None = None, time_steps: int = 2):
     else:
         _, el = impl.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, time_steps, DT, threads=threads)
     cells = float(np.prod(SHAPE)) * time_steps
-    return {"value": cells / el / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
-            "sample": f"512^3 x {time_steps} time steps (of the workload's 100), "
-                      f"{el:.2f} s, OMP_NUM_THREADS={threads}, "
-                      + ("reference upwind.cxx compiled by oracle/Makefile" if kind == "reference"
-                         else "oracle C restatement, -O3 -fopenmp -ffp-contract=off")}
+    out = {"value": cells / el / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
+           "sample": f"{N_AXIS}^3 x {time_steps} time steps (of the workload's 100), "
+                     f"{el:.2f} s, OMP_NUM_THREADS={threads}, "
+                     + ("reference upwind.cxx compiled by oracle/Makefile" if kind == "reference"
+                        else "oracle C restatement, -O3 -fopenmp -ffp-contract=off")}
+    if one_thread:
+        # the same restatement on one core, one time step
+        _, el1 = port.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, 1, DT, threads=1)
+        out["one_thread"] = {"value": float(np.prod(SHAPE)) / el1 / 1e9, "unit": "GCUPS",
+                             "cores": 1, "kind": "port",
+                             "sample": f"{N_AXIS}^3 x 1 time step, {el1:.2f} s, 1 thread"}
+    return out
 
 
 BATCH_COUNT = 256
@@ -660,7 +668,7 @@ def main() -> None:
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_sample()
+        cpu = cpu_sample(one_thread=True)
 
     if rank == 0:
         line = {
