@@ -423,6 +423,60 @@ LAP_DIMS = 2
 LAP_ITERS = 10
 
 
+def bench_batch_adjoint(stream) -> dict:
+    """Batched adjoint with the velocity gradient: the recovery batch (64
+    instances of 128^3, seeded velocities in [-1, 1]^3 rescaled to a Courant
+    sum of 0.5, sphere fields), 100 steps, a seeded Gaussian lambda_T.  One
+    batched advect against the closed form (one transposed persistent launch,
+    one contraction launch, the forward) and the step-by-step form
+    (checkpoints every 10 steps, recompute and contraction per step)."""
+    import torch
+    import fidibench_gb300 as fdb
+    from fidibench_gb300.recovery import instance_specs, sphere_field
+
+    count, n, steps = 64, 128, 100
+    specs = instance_specs(count, n, SEED)
+    dts = [sp["dt"] for sp in specs]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    f0 = torch.cat([sphere_field(n, sp["center"], sp["radius"], dev).view(-1) for sp in specs])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + 2)
+    lam = torch.randn(f0.numel(), generator=gen, device=dev, dtype=torch.float64)
+    b = fdb.Batch([(sp["v"], (1.0, 1.0, 1.0), (n, n, n)) for sp in specs])
+    b.set_stream(stream)
+
+    def timed(fn, reps=2):
+        fn()
+        ms = []
+        for _ in range(reps):
+            b.set_fields(f0)
+            stream.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return min(ms), out
+
+    b.set_fields(f0)
+    adv_ms, _ = timed(lambda: b.advect(steps, dts))
+    b.set_adjoint_form("closed")
+    b.set_fields(f0)
+    cl_ms, (_, gv_c) = timed(lambda: b.adjoint(steps, dts, lam))
+    b.set_adjoint_form("stepwise")
+    b.set_fields(f0)
+    sw_ms, (_, gv_s) = timed(lambda: b.adjoint(steps, dts, lam, checkpoint_every=10))
+    b.close()
+    rel = float(np.max(np.abs(gv_c - gv_s)) / np.max(np.abs(gv_s)))
+    return {"workload": "batch64_128cube_100steps", "instances": count,
+            "advect_ms": adv_ms, "closed_ms": cl_ms, "stepwise_ms": sw_ms,
+            "closed_over_advect": cl_ms / adv_ms, "stepwise_over_advect": sw_ms / adv_ms,
+            "grad_v_rel_diff": rel,
+            "timing": "CUDA events around each call, host-synchronising calls included"}
+
+
 def bench_laplacian(stream, cpu: bool) -> dict:
     """Stencil Filter: the reference laplacian driver's default case, 2-D
     8000^2 on the unit square, input prod_i sin(2 pi x_i) at the cell centres,
@@ -662,6 +716,7 @@ def main() -> None:
         # 100 steps, 20 gradient-descent iterations through the autograd Function
         from fidibench_gb300.recovery import recover
         recovery = recover(count=64, n=128, steps=100, iters=20, seed=SEED)
+        recovery["batched_adjoint_with_velocity"] = bench_batch_adjoint(stream)
     laplacian = None
     if not args.no_laplacian and rank == 0:
         laplacian = bench_laplacian(stream, cpu=not args.no_cpu_baseline)
