@@ -143,3 +143,40 @@ def test_adjoint_oracle_velocity_gradient_fd(port):
         jm = float(lam @ port.advect(n, vm, L, f, 1, dt))
         dcdv = dt * (1.0 if v[j] < 0 else -1.0) * n[j] / L[j]
         assert dcoef[j] * dcdv == pytest.approx((jp - jm) / (2 * h), rel=1e-6)
+
+
+@pytest.mark.parametrize("n,v,cfl", [((6, 7, 8), (0.7, -0.5, 0.35), 0.4),
+                                     ((5, 6, 7), (1.0, 1.0, 1.0), 0.5),  # sum a = 1.5 > 1
+                                     ((6, 5, 9), (0.5, 0.0, -0.5), 0.45),
+                                     ((9, 11), (0.6, -0.8), 0.4),
+                                     ((17,), (-0.5,), 0.7)])
+def test_closed_form_velocity_gradient_identity(port, n, v, cfl):
+    """On the periodic grid with constant coefficients the step's operators
+    commute, so the per-step velocity contractions of the reverse sweep sum to
+    S <lam^1, D_j f0> with lam^1 = (A^T)^(S-1) lam_T.  Checked on the oracle's
+    own FP64 step and transposed step (no GPU)."""
+    L = (1.0,) * len(n)
+    dt = cfl * min(Lj / nj / abs(vj) for Lj, nj, vj in zip(L, n, v) if vj != 0.0)
+    S = 9
+    rng = np.random.default_rng(sum(n) + S)
+    f0 = rng.standard_normal(int(np.prod(n)))
+    lam_t = rng.standard_normal(f0.size)
+    states = [f0]
+    for _ in range(S - 1):
+        states.append(port.advect(n, v, L, states[-1], 1, dt))
+    lam = lam_t.copy()
+    dcoef = np.zeros(len(n))
+    for k in range(S - 1, -1, -1):
+        lam, dc = port.adjoint_step(n, v, L, dt, states[k], lam)
+        dcoef += dc
+        if k == 1:
+            lam1 = lam.copy()
+    if S == 1:
+        lam1 = lam_t
+    f = f0.reshape(n)
+    closed = np.empty(len(n))
+    for j in range(len(n)):
+        up = 1 if v[j] < 0 else -1
+        dj = (np.roll(f, -up, axis=j) - f).reshape(-1)  # f[i + up_j e_j] - f[i]
+        closed[j] = -S * float(lam1 @ dj)
+    assert np.allclose(closed, dcoef, rtol=1e-12, atol=1e-12 * np.abs(dcoef).max())
