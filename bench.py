@@ -550,27 +550,66 @@ def bench_laplacian(stream, cpu: bool) -> dict:
     return out
 
 
+REF_TIME_STEPS_PER_BENCH_STEP = 10  # the reference arm's bounded sample per bench step
+
+
+def bench_config(ws: int) -> dict:
+    """The workload's config, identical in both arms."""
+    return {"workload": WORKLOAD, "shape": list(SHAPE), "velocity": list(VELOCITY),
+            "time_steps": TIME_STEPS, "dt": DT,
+            "init": f"sphere r={RADIUS} + U[0,{NOISE}) noise, seed {SEED}",
+            "l2": "inputs larger than L2 (1 GiB field per buffer)",
+            "parallelism": f"replicas x{ws}"}
+
+
 def run_reference_arm(args, ws, rank) -> None:
+    """The reference's CPU implementation of the path on the host cores: each
+    bench step runs advect() over REF_TIME_STEPS_PER_BENCH_STEP of the
+    workload's 100 time steps of the full 512^3 field (all host threads);
+    `ms_per_step` is the wall time one such bench step measured, and `value`
+    the cell-update rate over all timed bench steps."""
     if rank != 0:
         return
+    from oracle import Port, Reference
     threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    port = Port()
+    f0 = port.sphere_noise(SHAPE, LENGTHS, CENTER, RADIUS, NOISE, SEED)
+    kind, impl = "port", port
+    if Reference.available():
+        try:
+            impl, kind = Reference(), "reference"
+        except OSError:
+            impl, kind = port, "port"
+    nts = REF_TIME_STEPS_PER_BENCH_STEP
+
+    def one_step() -> float:
+        if kind == "reference":
+            _, el = impl.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, nts, DT)
+        else:
+            _, el = impl.advect_timed(SHAPE, VELOCITY, LENGTHS, f0, nts, DT, threads=threads)
+        return el
+
     for _ in range(args.warmup):
-        cpu_sample(threads, time_steps=1)
-    vals = [cpu_sample(threads, time_steps=1) for _ in range(args.steps)]
-    v = statistics.median(x["value"] for x in vals)
-    base = dict(vals[0])
-    base["value"] = v
-    base["sample"] = f"512^3 x 1 time step per bench step, median of {args.steps}; " + \
-        base["sample"].split(", ", 1)[1]
-    ms = float(np.prod(SHAPE)) * TIME_STEPS / (v * 1e9) * 1e3
+        one_step()
+    times = [one_step() for _ in range(args.steps)]
+    total = sum(times)
+    cells = float(np.prod(SHAPE))
+    v = cells * nts * args.steps / total / 1e9
+    what = ("reference upwind.cxx compiled by oracle/Makefile" if kind == "reference"
+            else "oracle C restatement, -O3 -fopenmp -ffp-contract=off")
+    sample = (f"{N_AXIS}^3 x {nts} time steps (of the workload's {TIME_STEPS}) per bench step, "
+              f"{args.steps} bench steps in {total:.2f} s, OMP_NUM_THREADS={threads}, {what}")
     print(json.dumps({
         "impl": "reference", "metric": "FP64 GCUPS (upwind advection, 512^3 periodic)",
         "value": v, "unit": "GCUPS", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "velocity": list(VELOCITY),
-                   "time_steps": TIME_STEPS, "dt": DT, "l2": "inputs larger than L2 (1 GiB field)"},
-        "cpu_baseline": base,
+        "warmup": args.warmup, "ms_per_step": total * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "arith": "f64 (the reference's operation order)",
+        "time_steps_timed": nts,
+        "config": bench_config(ws),
+        "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -585,6 +624,8 @@ def main() -> None:
     ap.add_argument("--depth", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-f64-paths", action="store_true",
+                    help="skip the FP64 (exact/fma) arithmetic figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-looped leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-recovery", action="store_true",
@@ -701,6 +742,27 @@ def main() -> None:
                "api": "Upwind.advect_host_stream (fdb_upwind_advect_host_stream)",
                "serial_value": ws * cells * TIME_STEPS * args.steps / el_serial / 1e9,
                "serial_api": "set_field + advect + get_field + checksum per step"}
+    # ---- the per-cell FP64 arithmetics beside the headline -----------------------------
+    f64_paths = None
+    if not args.no_f64_paths:
+        f64_paths = {}
+        for name in ("fma", "exact"):
+            up.set_arith(name)
+            up.init_sphere(CENTER, RADIUS, NOISE, SEED)
+            up.advect(10, DT)  # warm-up
+            stream.synchronize()
+            e0.record(stream)
+            up.advect(TIME_STEPS, DT)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            g = cells * TIME_STEPS / (ms * 1e-3) / 1e9
+            f64_paths[name] = {"gcups": g, "ms_per_advect": ms,
+                               "frac_of_16B_roofline": g * BYTES_PER_CELL_UPDATE / peak}
+        f64_paths["note"] = ("FP64 arithmetic per cell: exact = the reference's operation "
+                             "order (bit-identical), fma = 1 DMUL + 3 DFMA; one advect of "
+                             f"{TIME_STEPS} steps each, device-timed")
+        up.set_arith(args.arith, args.depth)
     up.close()
 
     batched = None
@@ -732,12 +794,8 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if arith_used != "fixed" else "f64 (i64 block-fixed-point arithmetic)",
-            "data": "synthetic",
-            "config": {"workload": WORKLOAD, "shape": list(SHAPE), "velocity": list(VELOCITY),
-                       "time_steps": TIME_STEPS, "dt": DT, "arith": arith_used,
-                       "init": "sphere r=0.2 + U[0,0.01) noise, seed 20261203",
-                       "l2": "inputs larger than L2 (1 GiB field per buffer)",
-                       "parallelism": f"replicas x{ws}"},
+            "data": "synthetic", "arith": arith_used, "time_steps_timed": TIME_STEPS,
+            "config": bench_config(ws),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": None if tpc is None else tpc * cell_updates_per_launch,
@@ -745,6 +803,7 @@ def main() -> None:
                          "basis": "16 B algorithmic per cell-update"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "f64_paths": f64_paths,
             "clocks": clk,
             "gpu_launches": launches,
             "batched": batched,

@@ -30,6 +30,12 @@ ARITH_FMA = 2
 ARITH_FIXED = 3
 ARITH_NAMES = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fma": ARITH_FMA, "fixed": ARITH_FIXED}
 
+COEFF_CXX = 0
+COEFF_PRODUCT = 1
+# "python": the reference's Python class rounds its coefficients as the
+# OpenACC/OpenMP-offload variants do
+COEFF_NAMES = {"cxx": COEFF_CXX, "product": COEFF_PRODUCT, "python": COEFF_PRODUCT}
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _vp = ctypes.c_void_p
@@ -53,6 +59,7 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_set_stream": (_int, [_vp, _vp]),
     "fdb_upwind_set_velocity": (_int, [_vp, _vp]),
     "fdb_upwind_set_arith": (_int, [_vp, _int, _int]),
+    "fdb_upwind_set_coeff_form": (_int, [_vp, _int]),
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),
     "fdb_checksum_noalloc": (_int, [_vp, ctypes.c_uint64, _vp, _vp]),

@@ -699,11 +699,11 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
   for (int sgi = io.nseg - 1; sgi >= 0; --sgi) {
     const int len = std::min(io.K, io.S - sgi * io.K);
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
-    if (io.recompute_ev) {
-      cudaEventCreate(&e0);
-      cudaEventCreate(&e1);
-      cudaEventCreate(&e2);
-      cudaEventRecord(e0, st);
+    if (io.events && (io.recompute_ev || io.adjoint_ev)) {
+      e0 = io.events->make();
+      e1 = io.events->make();
+      e2 = io.events->make();
+      EventPool::record(e0, st);
     }
     {
       NvtxScope nvtx_r("fdb.adjoint.recompute");
@@ -728,10 +728,8 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       }
     }
     FDB_CUDA_TRY(cudaGetLastError());
-    if (io.recompute_ev) {
-      cudaEventRecord(e1, st);
-      io.recompute_ev->push_back({e0, e1});
-    }
+    EventPool::record(e1, st);
+    if (io.recompute_ev && e0 && e1) io.recompute_ev->push_back({e0, e1});
     NvtxScope nvtx_t("fdb.adjoint.transposed");
     // adjoint steps n = sK+len-1 .. sK
     for (int k = len - 1; k >= 0; --k) {
@@ -746,10 +744,8 @@ int adjoint_fixed_run(const AdjointFixedIO& io, cudaStream_t st) {
       lc ^= 1;
       ++li;
     }
-    if (io.adjoint_ev) {
-      cudaEventRecord(e2, st);
-      io.adjoint_ev->push_back({e1, e2});
-    }
+    EventPool::record(e2, st);
+    if (io.adjoint_ev && e1 && e2) io.adjoint_ev->push_back({e1, e2});
   }
   k_to_double<<<grid_for(n), 256, 0, st>>>(io.lam[lc], io.grad_f0, n, lr + (li % 3));
   k_sum3<<<1, 256, 0, st>>>(io.dpart, nblk, io.dda3);

@@ -1274,9 +1274,12 @@ int fdb_batch_autotune(fdb_batch* b, int num_steps, const double* dt, const char
   FDB_CUDA_TRY(cudaMemcpyAsync(save, b->arena[b->cur], b->total * 8, cudaMemcpyDeviceToDevice,
                                b->stream));
   const int cur0 = b->cur;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  EventPool events;
+  cudaEvent_t e0 = events.make(), e1 = events.make();
+  if (!e0 || !e1) {
+    cudaFree(save);
+    return fail(FDB_ERR_CUDA, "autotune: cudaEventCreate failed");
+  }
   float best = 1e30f;
   int bK = 4, bsh = fx::kR4W8S, btz = 0;
   int rc = FDB_OK;
@@ -1308,8 +1311,6 @@ int fdb_batch_autotune(fdb_batch* b, int num_steps, const double* dt, const char
   cudaMemcpyAsync(b->arena[cur0], save, b->total * 8, cudaMemcpyDeviceToDevice, b->stream);
   cudaStreamSynchronize(b->stream);
   cudaFree(save);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rc) return rc;
   b->K = bK;
   b->shape = bsh;

@@ -123,6 +123,12 @@ int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Ge
 }
 
 double ref_coeff(const Geom& g, int j, double dt) {
+  if (g.coeff_form == FDB_COEFF_PRODUCT) {
+    // coeff[j] = v[j] * upDirection[j] / deltas[j] in the constructor, then
+    // deltaTime * coeff[j] per update (upwindAcc.cxx:45,79; upwind.py:32,64)
+    const double k = g.v[j] * (double)g.up[j] / g.dx[j];
+    return dt * k;
+  }
   // deltaTime * this->v[j] * this->upDirection[j] / this->deltas[j]
   return dt * g.v[j] * (double)g.up[j] / g.dx[j];
 }
@@ -648,7 +654,16 @@ int fdb_upwind_set_velocity(fdb_upwind* h, const double* velocity) {
   if (!velocity) return fail(FDB_ERR_INVALID, "null velocity");
   Geom g;
   FDB_TRY(make_geom(h->g.ndims, velocity, h->g.L, h->g.n, &g));
+  g.coeff_form = h->g.coeff_form;
   h->g = g;
+  return FDB_OK;
+}
+
+int fdb_upwind_set_coeff_form(fdb_upwind* h, int form) {
+  FDB_TRY(check_handle(h));
+  if (form != FDB_COEFF_CXX && form != FDB_COEFF_PRODUCT)
+    return fail(FDB_ERR_INVALID, "coefficient form must be FDB_COEFF_CXX or FDB_COEFF_PRODUCT");
+  h->g.coeff_form = form;
   return FDB_OK;
 }
 
@@ -811,11 +826,11 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
       return rc;
     }
   }
-  // forward with checkpoints: ckpt[s] = f^{sK}
-  cudaEvent_t fe0, fe1;
-  cudaEventCreate(&fe0);
-  cudaEventCreate(&fe1);
-  cudaEventRecord(fe0, h->stream);
+  // forward with checkpoints: ckpt[s] = f^{sK}.  Every timing event of the
+  // call lives in `events` and is destroyed on every return path.
+  EventPool events;
+  cudaEvent_t fe0 = events.make(), fe1 = events.make();
+  EventPool::record(fe0, h->stream);
   {
     NvtxScope nvtx_f("fdb.adjoint.forward");
     for (int s = 0; s < nseg; ++s) {
@@ -825,23 +840,18 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
       FDB_TRY(advance(h, len, dt, arith));
     }
   }
-  cudaEventRecord(fe1, h->stream);
+  EventPool::record(fe1, h->stream);
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rec_ev, adj_ev;
   auto collect_times = [&]() {
     float ms = 0.f;
     h->adj_ms[0] = h->adj_ms[1] = h->adj_ms[2] = 0.0;
-    if (cudaEventElapsedTime(&ms, fe0, fe1) == cudaSuccess) h->adj_ms[0] = ms;
+    if (fe0 && fe1 && cudaEventElapsedTime(&ms, fe0, fe1) == cudaSuccess) h->adj_ms[0] = ms;
     for (auto& e : rec_ev) {
       if (cudaEventElapsedTime(&ms, e.first, e.second) == cudaSuccess) h->adj_ms[1] += ms;
     }
     for (auto& e : adj_ev) {
       if (cudaEventElapsedTime(&ms, e.first, e.second) == cudaSuccess) h->adj_ms[2] += ms;
-      cudaEventDestroy(e.second);
     }
-    for (auto& e : rec_ev) cudaEventDestroy(e.first);
-    for (auto& e : rec_ev) cudaEventDestroy(e.second);
-    cudaEventDestroy(fe0);
-    cudaEventDestroy(fe1);
     cudaGetLastError();
   };
   double dda[3] = {0.0, 0.0, 0.0};  // dL/da (internal axes z, y, x)
@@ -892,6 +902,7 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
     io.scratch = h->adj_scratch;
     io.recompute_ev = &rec_ev;
     io.adjoint_ev = &adj_ev;
+    io.events = &events;
     FDB_TRY(adjoint_fixed_run(io, h->stream));
     if (!is_device)
       FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -914,11 +925,9 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
                                  is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                  h->stream));
     FDB_CUDA_TRY(cudaMemsetAsync(h->dpart, 0, 3 * adjoint_blocks() * sizeof(double), h->stream));
-    cudaEvent_t be0, be1;
-    cudaEventCreate(&be0);
-    cudaEventCreate(&be1);
-    cudaEventRecord(be0, h->stream);
-    adj_ev.push_back({be0, be1});
+    cudaEvent_t be0 = events.make(), be1 = events.make();
+    EventPool::record(be0, h->stream);
+    if (be0 && be1) adj_ev.push_back({be0, be1});
     rec_ev.clear();
     for (int s = nseg - 1; s >= 0; --s) {
       const int len = std::min(K, S - s * K);
@@ -934,7 +943,7 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
         lc ^= 1;
       }
     }
-    cudaEventRecord(be1, h->stream);
+    EventPool::record(be1, h->stream);
     FDB_CUDA_TRY(cudaMemcpyAsync(grad_f0, h->lam[lc], bytes,
                                  is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                  h->stream));
@@ -943,7 +952,6 @@ int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* la
                                  h->stream));
     FDB_TRY(sync(h));
     collect_times();
-    cudaEventDestroy(be0);
     // the FP64 kernel accumulates dL/dc = -dL/da
     for (int k = 0; k < 3; ++k) dda[k] = -h->hscal[k];
   }

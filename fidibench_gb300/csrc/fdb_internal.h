@@ -48,6 +48,31 @@ struct NvtxScope {
   NvtxScope& operator=(const NvtxScope&) = delete;
 };
 
+// Timing events of one call: every event the call creates comes from here and
+// is destroyed when the pool goes out of scope, on every return path.
+struct EventPool {
+  std::vector<cudaEvent_t> all;
+  EventPool() = default;
+  EventPool(const EventPool&) = delete;
+  EventPool& operator=(const EventPool&) = delete;
+  ~EventPool() {
+    for (cudaEvent_t e : all) cudaEventDestroy(e);
+  }
+  // null when creation fails (the timings then read as 0)
+  cudaEvent_t make() {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    all.push_back(e);
+    return e;
+  }
+  static void record(cudaEvent_t e, cudaStream_t s) {
+    if (e) cudaEventRecord(e, s);
+  }
+};
+
 // Geometry of one problem, normalised to 3 internal axes (z, y, x) = reference
 // axes (ndims-3, ndims-2, ndims-1); missing leading axes have extent 1 and
 // zero velocity.  Problems with more than 3 axes use the generic kernels.
@@ -64,11 +89,13 @@ struct Geom {
   int64_t nz = 1, ny = 1, nx = 1;
   int upz = -1, upy = -1, upx = -1;
   int jz = -1, jy = -1, jx = -1;  // reference axis of each internal axis (-1: padded)
+  int coeff_form = FDB_COEFF_CXX;  // how ref_coeff rounds c_j (FDB_COEFF_*)
 };
 
 int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g);
 
-// The reference coefficient of axis j: ((dt * v_j) * up_j) / dx_j  (upwind.cxx:72).
+// The reference coefficient of axis j: ((dt * v_j) * up_j) / dx_j (upwind.cxx:72),
+// or dt * ((v_j * up_j) / dx_j) under FDB_COEFF_PRODUCT (upwindAcc.cxx:45,79).
 double ref_coeff(const Geom& g, int j, double dt);
 
 // The geometry of the transposed step: every upwind direction reversed
@@ -173,9 +200,11 @@ struct AdjointFixedIO {
   double* dda3;            // device [3]: dL/da for the internal (z, y, x) axes
   void* scratch;           // adjoint_fixed_scratch_bytes(K) bytes
   // nullable: event pairs bracketing each recompute / transposed-step block,
-  // for the caller to read after it synchronises
+  // for the caller to read after it synchronises; the events come from (and
+  // are owned by) `events`, which must be set when either list is
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* recompute_ev = nullptr;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* adjoint_ev = nullptr;
+  EventPool* events = nullptr;
 };
 size_t adjoint_fixed_scratch_bytes(int seg_len);
 // ntot-double buffers the fixed-point adjoint needs for a segment of K steps:

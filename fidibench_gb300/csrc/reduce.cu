@@ -136,6 +136,7 @@ int launch_std(const double* f, uint64_t n, double* part, double* d_tmp, double*
 // from different host threads) race and must be serialised by the caller.
 // ---------------------------------------------------------------------------
 #include <mutex>
+#include <string>
 
 namespace {
 
@@ -165,6 +166,28 @@ int noalloc_scratch(double** out) {
   return FDB_OK;
 }
 
+// The kernels dereference d_field and d_sum on the current device: a host
+// pointer, or memory of another GPU, would fault there instead of failing
+// here.  cudaPointerGetAttributes only reads the driver's records (it
+// allocates nothing).
+int check_on_current_device(const void* p, const char* what) {
+  int dev = 0;
+  FDB_CUDA_TRY(cudaGetDevice(&dev));
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fdb::fail(FDB_ERR_INVALID, std::string("fdb_checksum_noalloc: ") + what +
+                                          " is not a pointer the CUDA runtime knows");
+  }
+  const bool on_device = at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (!on_device || at.device != dev)
+    return fdb::fail(FDB_ERR_INVALID, std::string("fdb_checksum_noalloc: ") + what +
+                                          " must be device (or managed) memory of the current "
+                                          "device");
+  return FDB_OK;
+}
+
 }  // namespace
 
 extern "C" int fdb_checksum_noalloc(const double* d_field, uint64_t n, double* d_sum,
@@ -179,5 +202,7 @@ extern "C" int fdb_checksum_noalloc(const double* d_field, uint64_t n, double* d
                                       "than the 2048-entry static scratch holds");
   double* part = nullptr;
   FDB_TRY(noalloc_scratch(&part));
+  FDB_TRY(check_on_current_device(d_field, "d_field"));
+  FDB_TRY(check_on_current_device(d_sum, "d_sum"));
   return fdb::launch_sum(d_field, n, part, d_sum, (cudaStream_t)cuda_stream);
 }

@@ -43,7 +43,8 @@ def _order_after_torch(t) -> None:
 class Upwind:
     """Periodic N-D first-order upwind advection of a scalar field (FP64)."""
 
-    def __init__(self, velocity, lengths, numCells, arith: str = "auto", depth: int = 0):
+    def __init__(self, velocity, lengths, numCells, arith: str = "auto", depth: int = 0,
+                 coeff_form: str = "cxx"):
         self.v = _as_f64(velocity)
         self.lengths = _as_f64(lengths)
         self.numCells = [int(x) for x in numCells]
@@ -60,6 +61,8 @@ class Upwind:
         self.upDirection = np.where(self.v < 0.0, 1, -1).astype(np.int32)
         self.deltas = self.lengths / np.asarray(self.numCells, dtype=np.float64)
         self.set_arith(arith, depth)
+        if coeff_form != "cxx":
+            self.set_coeff_form(coeff_form)
 
     # -- lifetime ---------------------------------------------------------------
     def close(self) -> None:
@@ -83,6 +86,13 @@ class Upwind:
     def set_arith(self, arith: str = "auto", depth: int = 0) -> None:
         code = _capi.ARITH_NAMES[arith] if isinstance(arith, str) else int(arith)
         check(lib.fdb_upwind_set_arith(self._h, code, int(depth)))
+
+    def set_coeff_form(self, form: str = "cxx") -> None:
+        """Rounding of the per-axis coefficient: "cxx" = ((dt*v)*up)/dx as
+        upwind/cxx/upwind.cxx:72 (default); "python" (or "product") =
+        dt*((v*up)/dx) as upwind/python/upwind.py:32,64 and the OpenACC
+        variants.  With arith="exact" each is bit-identical to its variant."""
+        check(lib.fdb_upwind_set_coeff_form(self._h, _capi.COEFF_NAMES[form]))
 
     def set_tile_z(self, tile_z: int) -> None:
         """Most output planes one CTA of the fixed-point kernel takes along
@@ -339,7 +349,8 @@ def main(argv=None) -> int:
     for j in range(ndims):
         dx = lengths[j] / float(numCells[j])
         dt = min(courant * dx / velocity[j], dt)
-    up = Upwind(velocity, lengths, numCells)
+    # the Python class rounds its coefficients as dt * (v*up/dx) (upwind.py:32,64)
+    up = Upwind(velocity, lengths, numCells, coeff_form="python")
     for _ in range(numTimeSteps):
         up.advect(dt)
     print("check sum: ", up.checksum())

@@ -117,6 +117,21 @@ int fdb_upwind_std(fdb_upwind* h, double* out);
  * kept.  Lets optimisation loops reuse one handle. */
 int fdb_upwind_set_velocity(fdb_upwind* h, const double* velocity);
 
+/* How the per-axis coefficient c_j of the update f -= c_j (f_up - f) is
+ * rounded from dt, v_j, up_j and dx_j.  The reference's variants differ:
+ *  FDB_COEFF_CXX     : c_j = ((dt * v_j) * up_j) / dx_j, evaluated per step
+ *                      (upwind/cxx/upwind.cxx:72; the default).
+ *  FDB_COEFF_PRODUCT : c_j = dt * ((v_j * up_j) / dx_j), with the bracket
+ *                      precomputed in the constructor (upwindAcc.cxx:45,79,
+ *                      upwindAcc2.cxx:48,85, upwindOMP5.cxx:46,86 and the
+ *                      Python class, upwind/python/upwind.py:32,64).
+ * Under FDB_ARITH_EXACT each form is bit-identical to the variant that uses
+ * it; the two differ by rounding only.  Applies to this handle's advect,
+ * adjoint and transposed runs. */
+#define FDB_COEFF_CXX 0
+#define FDB_COEFF_PRODUCT 1
+int fdb_upwind_set_coeff_form(fdb_upwind* h, int form);
+
 /* Stream to enqueue on (a cudaStream_t; NULL restores the handle's own). */
 int fdb_upwind_set_stream(fdb_upwind* h, void* cuda_stream);
 
@@ -286,9 +301,10 @@ int fdb_batch_autotune(fdb_batch* b, int num_steps, const double* dt, const char
  * or arena that owns all device memory, a host that forbids allocation after
  * start-up, a callback where cudaMalloc would synchronise or fail).
  *
- * Sums n FP64 values at d_field (device memory) into *d_sum (device memory),
- * enqueued on cuda_stream (a cudaStream_t; NULL = legacy default stream) and
- * not synchronised.  Same kernels and chunking as fdb_upwind_checksum, so the
+ * Sums n FP64 values at d_field into *d_sum, enqueued on cuda_stream (a
+ * cudaStream_t; NULL = legacy default stream) and not synchronised.  Both
+ * pointers must be device (or managed) memory of the current device; host
+ * memory or another GPU's memory returns FDB_ERR_INVALID.  Same kernels and chunking as fdb_upwind_checksum, so the
  * same result.  Scratch is a 2048-double (16 KB) static device array that the
  * library keeps on every GPU it is loaded on until the process exits; nothing
  * in it needs clearing between calls.  Calls that overlap on the GPU share the

@@ -2,10 +2,16 @@
 // rebuilt on the C-ABI of libfdb_upwind (include/fdb_upwind.h).
 //
 // Same constructor and member signatures as the reference, so a driver written
-// against upwind.cxx compiles against this header unchanged:
+// against upwind.cxx (or its OpenACC variants) compiles against this header
+// unchanged:
 //   Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
 //          const std::vector<size_t>& numCells)                 upwind.cxx:23-49
-//   void   advect(int numTimeSteps, double deltaTime)           upwind.cxx:51-86
+//   Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
+//          const std::vector<int>& numCells)                    upwindAcc.cxx:17-47,
+//                                                               upwindAcc2.cxx:18-50
+//   void   advect(int numTimeSteps, double deltaTime)           upwind.cxx:51-86,
+//                                                               upwindAcc2.cxx:52-99
+//   void   advect(double deltaTime)      (one step)             upwindAcc.cxx:49-90
 //   void   saveVTK(const std::string& filename)                 saveVTK.h:1-60
 //   double checksum() const                                     upwind.cxx:91-93
 //   double std() const                                          upwind.cxx:95-103
@@ -44,16 +50,23 @@ class Upwind {
   Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
          const std::vector<size_t>& numCells)
       : v_(velocity), lengths_(lengths), numCells_(numCells) {
-    if (velocity.size() < NDIMS || lengths.size() < NDIMS || numCells.size() < NDIMS)
-      throw std::invalid_argument("Upwind: need NDIMS velocity, lengths and numCells entries");
-    std::vector<uint64_t> n(numCells.begin(), numCells.begin() + NDIMS);
-    check(fdb_upwind_create((int)NDIMS, velocity.data(), lengths.data(), n.data(), &h_),
-          "fdb_upwind_create");
-    ntot_ = 1;
-    for (size_t j = 0; j < NDIMS; ++j) {
-      deltas_.push_back(lengths[j] / numCells[j]);
-      ntot_ *= numCells[j];
+    create();
+  }
+
+  // The OpenACC variants' constructor.  They precompute v_j * up_j / dx_j and
+  // multiply by deltaTime in each update (upwindAcc.cxx:45,79), a coefficient
+  // rounding that differs from upwind.cxx:72 in the last bit; the handle is
+  // set to that form (FDB_COEFF_PRODUCT), so FDB_ARITH_EXACT reproduces these
+  // variants bit for bit.
+  Upwind(const std::vector<double>& velocity, const std::vector<double>& lengths,
+         const std::vector<int>& numCells)
+      : v_(velocity), lengths_(lengths) {
+    for (int n : numCells) {
+      if (n <= 0) throw std::invalid_argument("Upwind: numCells must be positive");
+      numCells_.push_back((size_t)n);
     }
+    create();
+    check(fdb_upwind_set_coeff_form(h_, FDB_COEFF_PRODUCT), "fdb_upwind_set_coeff_form");
   }
   ~Upwind() { fdb_upwind_destroy(h_); }
   Upwind(const Upwind&) = delete;
@@ -62,6 +75,9 @@ class Upwind {
   void advect(int numTimeSteps, double deltaTime) {
     check(fdb_upwind_advect(h_, numTimeSteps, deltaTime), "fdb_upwind_advect");
   }
+
+  // One time step (upwindAcc.cxx:49-90).
+  void advect(double deltaTime) { advect(1, deltaTime); }
 
   double checksum() const {
     double s = 0.0;
@@ -166,10 +182,28 @@ class Upwind {
     check(fdb_upwind_set_arith(h_, arith, temporalDepth), "fdb_upwind_set_arith");
   }
 
+  // FDB_COEFF_CXX or FDB_COEFF_PRODUCT (fdb_upwind_set_coeff_form).
+  void setCoeffForm(int form) {
+    check(fdb_upwind_set_coeff_form(h_, form), "fdb_upwind_set_coeff_form");
+  }
+
   fdb_upwind* handle() { return h_; }
   size_t size() const { return ntot_; }
 
  private:
+  void create() {
+    if (v_.size() < NDIMS || lengths_.size() < NDIMS || numCells_.size() < NDIMS)
+      throw std::invalid_argument("Upwind: need NDIMS velocity, lengths and numCells entries");
+    std::vector<uint64_t> n(numCells_.begin(), numCells_.begin() + NDIMS);
+    check(fdb_upwind_create((int)NDIMS, v_.data(), lengths_.data(), n.data(), &h_),
+          "fdb_upwind_create");
+    ntot_ = 1;
+    for (size_t j = 0; j < NDIMS; ++j) {
+      deltas_.push_back(lengths_[j] / numCells_[j]);
+      ntot_ *= numCells_[j];
+    }
+  }
+
   void axis(std::fstream& file, const char* label, int k) const {
     file << "\n" << label << " ";
     if (k < 0) {

@@ -19,16 +19,26 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfdb_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfdb_refupwind.so")
 REF_EXE = os.path.join(HERE, "_ref", "upwindCxx")
+REF_ACC_SO = os.path.join(HERE, "_ref", "libfdb_refacc.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def reference_dir() -> str:
+    """The reference's source tree: $FDB_REFERENCE_DIR, else a folder named
+    `reference` beside this repository's root (it may not exist)."""
+    env = os.environ.get("FDB_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 def build(ref: bool | None = None) -> None:
     """Compile the restatement (always) and the reference harness (when the
     reference source tree is present) with oracle/Makefile."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    refdir = os.environ.get("FDB_REFERENCE_DIR", "/root/reference")
+    refdir = reference_dir()
     if ref is None:
         ref = os.path.isfile(os.path.join(refdir, "upwind", "cxx", "upwind.cxx"))
     if ref:
@@ -57,6 +67,10 @@ class Port:
         lib.fdbo_advect.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp, _dp,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_int]
         lib.fdbo_advect.restype = ctypes.c_int
+        lib.fdbo_advect_form.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp, _dp,
+                                         ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_int]
+        lib.fdbo_advect_form.restype = ctypes.c_int
         lib.fdbo_checksum.argtypes = [_dp, ctypes.c_uint64]
         lib.fdbo_checksum.restype = ctypes.c_double
         lib.fdbo_std.argtypes = [_dp, ctypes.c_uint64]
@@ -74,10 +88,14 @@ class Port:
         lib.fdbo_max_threads.restype = ctypes.c_int
         self.lib = lib
 
-    def advect(self, n, v, L, f0, steps: int, dt: float, threads: int = 0) -> np.ndarray:
-        return self.advect_timed(n, v, L, f0, steps, dt, threads)[0]
+    def advect(self, n, v, L, f0, steps: int, dt: float, threads: int = 0,
+               coeff_form: int = 0) -> np.ndarray:
+        """coeff_form 0: the coefficient of upwind.cxx:72; 1: the product
+        form of the OpenACC variants and the Python class."""
+        return self.advect_timed(n, v, L, f0, steps, dt, threads, coeff_form)[0]
 
-    def advect_timed(self, n, v, L, f0, steps: int, dt: float, threads: int = 0):
+    def advect_timed(self, n, v, L, f0, steps: int, dt: float, threads: int = 0,
+                     coeff_form: int = 0):
         """(final field, wall seconds of the advect call alone)."""
         import time
         n, v, L = _u64(n), _f64(v), _f64(L)
@@ -85,8 +103,9 @@ class Port:
         scratch = np.empty_like(f)
         scratch.fill(0.0)  # fault the pages in outside the timed call
         t0 = time.perf_counter()
-        rc = self.lib.fdbo_advect(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
-                                  _ptr(f), _ptr(scratch), int(steps), float(dt), int(threads))
+        rc = self.lib.fdbo_advect_form(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                       _ptr(f), _ptr(scratch), int(steps), float(dt),
+                                       int(threads), int(coeff_form))
         el = time.perf_counter() - t0
         if rc:
             raise ValueError("oracle advect rejected its arguments")
@@ -240,6 +259,38 @@ class Reference:
         n = _u64(n)
         f = _f64(f).reshape(-1)
         return self.lib.fdbr_std(len(n), n.ctypes.data_as(_u64p), _ptr(f))
+
+
+class ReferenceAcc:
+    """The reference's OpenACC variants upwindAcc.cxx (variant 1: one-step
+    advect(double)) and upwindAcc2.cxx (variant 2: advect(int, double)),
+    compiled serially by ref_acc_harness.cpp, when built here.  3-D only."""
+
+    def __init__(self, path: str = REF_ACC_SO):
+        if not os.path.isfile(path):
+            raise FileNotFoundError(path)
+        lib = ctypes.CDLL(path)
+        lib.fdbr_acc_advect.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                        ctypes.c_double]
+        lib.fdbr_acc_advect.restype = ctypes.c_int
+        self.lib = lib
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.isfile(REF_ACC_SO)
+
+    def advect(self, variant: int, n, v, L, f0, steps: int, dt: float) -> np.ndarray:
+        n, v, L = _u64(n), _f64(v), _f64(L)
+        if len(n) != 3:
+            raise ValueError("the OpenACC variants are 3-D")
+        out = np.empty(int(np.prod(n)), dtype=np.float64)
+        fin = None if f0 is None else _f64(f0).reshape(-1)
+        rc = self.lib.fdbr_acc_advect(int(variant), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                      None if fin is None else _ptr(fin), _ptr(out), int(steps),
+                                      float(dt))
+        if rc:
+            raise ValueError("reference OpenACC harness rejected its arguments")
+        return out
 
 
 def reference_dt(n, v, L, courant: float) -> float:

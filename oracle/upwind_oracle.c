@@ -81,12 +81,37 @@ uint64_t fdbo_ntot(int ndims, const uint64_t *n) {
   return t;
 }
 
+/* The coefficient as the OpenACC/OpenMP-offload variants and the Python
+ * class round it: coeff[j] = v[j] * upDirection[j] / deltas[j] once in the
+ * constructor (upwindAcc.cxx:45, upwindAcc2.cxx:48, upwind.py:32), then
+ * deltaTime * coeff[j] in each update (upwindAcc.cxx:79, upwindAcc2.cxx:85,
+ * upwind.py:64). */
+double fdbo_coeff_product(double dt, double v, int up, double delta) {
+  const double k = v * (double)up / delta;
+  return dt * k;
+}
+
+/* advect with a choice of coefficient rounding: form 0 = upwind.cxx:72,
+ * form 1 = fdbo_coeff_product.  The update itself, f[i] -= c_j * (oldF[upI] -
+ * oldF[i]) axis by axis in order j = 0..ndims-1, is the same in every
+ * variant (upwind.cxx:80, upwindAcc.cxx:79-87, upwindAcc2.cxx:85-91,
+ * upwind.py:55-67). */
+int fdbo_advect_form(int ndims, const uint64_t *n, const double *v, const double *L,
+                     double *f, double *oldF, int numTimeSteps, double deltaTime,
+                     int nthreads, int form);
+
 /* One full advect(numTimeSteps, deltaTime) -- upwind.cxx:51-86.
  * f is updated in place; oldF is caller-provided scratch of ntot doubles.
  * nthreads <= 0 keeps the OpenMP default. Returns 0 on success. */
 int fdbo_advect(int ndims, const uint64_t *n, const double *v, const double *L,
                 double *f, double *oldF, int numTimeSteps, double deltaTime,
                 int nthreads) {
+  return fdbo_advect_form(ndims, n, v, L, f, oldF, numTimeSteps, deltaTime, nthreads, 0);
+}
+
+int fdbo_advect_form(int ndims, const uint64_t *n, const double *v, const double *L,
+                     double *f, double *oldF, int numTimeSteps, double deltaTime,
+                     int nthreads, int form) {
   fdbo_geom g;
   if (fdbo_geometry(ndims, n, v, L, &g)) return 1;
   const int64_t ntot = (int64_t)g.ntot;
@@ -110,7 +135,9 @@ int fdbo_advect(int ndims, const uint64_t *n, const double *v, const double *L,
         inds[d] = (int64_t)(((uint64_t)i / g.dimProd[d]) % g.n[d]);
       for (int j = 0; j < g.ndims; ++j) {
         int64_t oldIndex = inds[j];
-        const double coeff = deltaTime * g.v[j] * (double)g.up[j] / g.deltas[j];
+        const double coeff =
+            form == 1 ? fdbo_coeff_product(deltaTime, g.v[j], g.up[j], g.deltas[j])
+                      : deltaTime * g.v[j] * (double)g.up[j] / g.deltas[j];
         /* periodic BCs: upwind.cxx:75-76 */
         inds[j] = (inds[j] + g.up[j] + (int64_t)g.n[j]) % (int64_t)g.n[j];
         /* getFlatIndex: upwind.cxx:131-134 */

@@ -70,6 +70,31 @@ int main() {
   }
   CHECK(std::fabs((double)(lhs - rhs)) <= 1e-11 * std::fabs((double)lhs),
         "dot-product identity");
+  // the OpenACC variants' constructor (std::vector<int>, product coefficient
+  // form) and their one-step advect(double): under EXACT, S one-step calls
+  // give the field of one advect(S, dt) call bit for bit
+  {
+    const std::vector<int> ni = {16, 12, 20};
+    const double dt2 = 0.1 / 20;
+    fdb::Upwind<3> a(v, L, ni), b(v, L, ni);
+    a.setArith(FDB_ARITH_EXACT);
+    b.setArith(FDB_ARITH_EXACT);
+    for (int s = 0; s < 7; ++s) a.advect(dt2);
+    b.advect(7, dt2);
+    CHECK(a.getField() == b.getField(), "advect(double) x 7 equals advect(7, double)");
+    CHECK(a.size() == (size_t)16 * 12 * 20, "std::vector<int> constructor sizes the field");
+    std::vector<size_t> ns(ni.begin(), ni.end());
+    fdb::Upwind<3> c(v, L, ns);
+    c.setArith(FDB_ARITH_EXACT);
+    c.advect(7, dt2);
+    const std::vector<double> fa = a.getField(), fc = c.getField();
+    double num = 0.0, den = 0.0;
+    for (size_t i = 0; i < fa.size(); ++i) {
+      num = std::fmax(num, std::fabs(fa[i] - fc[i]));
+      den = std::fmax(den, std::fabs(fc[i]));
+    }
+    CHECK(num <= 1e-14 * den, "the two coefficient forms differ by rounding only");
+  }
   if (failures) return 1;
   std::printf("facade ok\n");
   return 0;

@@ -21,8 +21,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import Port, Reference, build, cfl_dt, reference_dt  # noqa: E402
+from oracle.oracle import reference_dir  # noqa: E402
 
-REFDIR = os.environ.get("FDB_REFERENCE_DIR", "/root/reference")
+REFDIR = reference_dir()
 SEED = 20261203
 
 
@@ -98,6 +99,31 @@ def python_reference_case() -> None:
          fT=up.f.copy(), checksum=np.float64(up.checksum()))
 
 
+def acc_cases(port: Port) -> None:
+    """The reference's OpenACC variants (upwindAcc.cxx: one advect(dt) call
+    per step; upwindAcc2.cxx: advect(steps, dt)), compiled serially by
+    oracle/ref_acc_harness.cpp: their drivers' own run (corner IC, v = 1,
+    courant 0.1, 16^3 x 10) and a mixed-sign seeded field (7 x 5 x 6)."""
+    from oracle.oracle import ReferenceAcc
+    acc = ReferenceAcc()
+    rng = np.random.default_rng(SEED + 7)
+    for variant in (1, 2):
+        n, v, L = (16, 16, 16), (1.0, 1.0, 1.0), (1.0, 1.0, 1.0)
+        dt = reference_dt(n, v, L, 0.1)
+        fT = acc.advect(variant, n, v, L, None, 10, dt)
+        save(f"acc{variant}_16cube_10", n=np.asarray(n, np.uint64), v=np.asarray(v, np.float64),
+             L=np.asarray(L, np.float64), dt=np.float64(dt), steps=np.int64(10), fT=fT,
+             checksum=np.float64(port.checksum(fT)))
+    n, v, L = (7, 5, 6), (0.8, -0.45, 0.3), (1.0, 2.0, 0.5)
+    f0 = rng.standard_normal(int(np.prod(n)))
+    dt = cfl_dt(n, v, L, 0.5)
+    fT = acc.advect(2, n, v, L, f0, 12, dt)
+    assert np.array_equal(fT, acc.advect(1, n, v, L, f0, 12, dt))
+    save("acc2_7x5x6_mixed", n=np.asarray(n, np.uint64), v=np.asarray(v, np.float64),
+         L=np.asarray(L, np.float64), dt=np.float64(dt), steps=np.int64(12), f0=f0, fT=fT,
+         checksum=np.float64(port.checksum(fT)))
+
+
 def vtk_case() -> None:
     """The reference driver binary (oracle/_ref/upwindCxx, built from the
     reference's own upwind.cxx + CmdLineArgParser.cpp) with -vtk -std: its
@@ -131,6 +157,7 @@ def main() -> None:
     field_cases(ref, port)
     driver_cases(ref)
     python_reference_case()
+    acc_cases(port)
     vtk_case()
     synth_case(port)
 

@@ -1,5 +1,6 @@
-"""Small stand-alone runs of one kernel family, for profiling a single launch
-on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
+"""Profiling harness: small stand-alone runs of one kernel family, for
+profiling a single launch on a case of a few hundred MB
+(python tests/profile_cases.py ...).  Not collected by pytest.
 
   adjoint N S [form] : N^3 field, v = (0.8, 0.5, -0.6), dt = 0.5 min(dx/|v|),
                 three adjoint calls of S steps; form "closed" (default: dL/dv
@@ -16,7 +17,12 @@ on a case of a few hundred MB (python -m fidibench_gb300.cases ...).
 """
 from __future__ import annotations
 
+import os
 import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
 
 def adjoint_case(n: int, steps: int, form: str = "closed") -> dict:

@@ -139,3 +139,49 @@ def test_cpp_facade_additions(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "facade ok" in r.stdout
+
+
+ACC_EXE = {name: os.path.join(ROOT, "fidibench_gb300", "_lib", name)
+           for name in ("upwindAccCxx", "upwindAcc2Cxx")}
+
+
+@pytest.mark.parametrize("name", ["upwindAccCxx", "upwindAcc2Cxx"])
+def test_ctest_acc_cases(name):
+    """upwind/cxx/CMakeLists.txt:93-107: `upwindAccCxx 32 10` and
+    `upwindAcc2Cxx 32 10`, same regex; the positional tokens are ignored, so
+    both run the default 128^3 x 10 (one advect(dt) call per step for Acc)."""
+    r = subprocess.run([ACC_EXE[name], "32", "10"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert CTEST_REGEX.search(r.stdout), r.stdout
+    assert "number of cells:  128 128 128" in r.stdout
+    assert "number of time steps: 10" in r.stdout
+
+
+@pytest.mark.parametrize("name,golden", [("upwindAccCxx", "acc1_16cube_10"),
+                                         ("upwindAcc2Cxx", "acc2_16cube_10")])
+def test_acc_driver_vtk_matches_reference_variant(tmp_path, fdb, name, golden):
+    """The driver's up.vtk under EXACT holds the reference variant's field
+    (the golden fixture, written with the same ASCII layout by the Python
+    mirror's writer for comparison)."""
+    g = load_golden(golden)
+    args = [ACC_EXE[name], "-numCells", "16", "-numSteps", "10", "-vtk", "-arith", "exact"]
+    if name == "upwindAcc2Cxx":
+        args.append("-std")
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert "check sum: 1\n" in r.stdout
+    if name == "upwindAcc2Cxx":
+        assert "std      : " in r.stdout
+    from fidibench_gb300.vtk import write_rectilinear
+    n = [int(x) for x in g["n"]]
+    write_rectilinear(str(tmp_path / "ref.vtk"), n, [1.0 / x for x in n], g["fT"],
+                      title="upwind.cxx")
+    assert (tmp_path / "up.vtk").read_text() == (tmp_path / "ref.vtk").read_text()
+
+
+def test_acc_driver_rejects_bad_option():
+    r = subprocess.run([ACC_EXE["upwindAccCxx"], "-std"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1
+    assert "-std is not a valid option." in r.stdout
+    assert "ERROR: wrong command line arguments" in r.stderr

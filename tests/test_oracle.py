@@ -92,6 +92,54 @@ def test_port_matches_reference_harness_random(port, reference):
         assert port.checksum(a) == reference.checksum(n, a)
 
 
+@pytest.mark.parametrize("name", ["acc1_16cube_10", "acc2_16cube_10", "acc2_7x5x6_mixed"])
+def test_port_product_form_matches_acc_golden_bit_exact(port, name):
+    """The product coefficient form (dt * (v*up/dx)) restates the OpenACC
+    variants upwindAcc.cxx / upwindAcc2.cxx bit for bit."""
+    g = load_golden(name)
+    n = [int(x) for x in g["n"]]
+    if "f0" in g:
+        f0 = g["f0"]
+    else:
+        f0 = np.zeros(int(np.prod(n)))
+        f0[0] = 1.0
+    out = port.advect(n, g["v"], g["L"], f0, int(g["steps"]), float(g["dt"]), coeff_form=1)
+    assert np.array_equal(out, g["fT"]), rel_maxnorm(out, g["fT"])
+    assert port.checksum(out) == float(g["checksum"])
+
+
+def test_port_product_form_matches_python_reference_bit_exact(port):
+    """The reference's Python class (upwind.py:32,64) rounds its coefficient
+    the same way: bit-identical under the product form."""
+    g = load_golden("python_12cube_10")
+    n = [int(x) for x in g["n"]]
+    f0 = np.zeros(int(np.prod(n)))
+    f0[0] = 1.0
+    out = port.advect(n, [1.0] * 3, [1.0] * 3, f0, int(g["steps"]), float(g["dt"]),
+                      coeff_form=1)
+    assert np.array_equal(out, g["fT"])
+
+
+def test_port_product_form_matches_acc_harness(port):
+    """Random 3-D cases against the reference's OpenACC variants compiled
+    here (skipped where they were not built)."""
+    from oracle.oracle import ReferenceAcc
+    if not ReferenceAcc.available():
+        pytest.skip("reference OpenACC harness not built in this tree")
+    acc = ReferenceAcc()
+    rng = np.random.default_rng(29)
+    for _ in range(12):
+        n = tuple(int(x) for x in rng.integers(1, 9, size=3))
+        v = tuple(float(x) for x in rng.uniform(-1.5, 1.5, size=3))
+        L = tuple(float(x) for x in rng.uniform(0.5, 2, size=3))
+        f0 = rng.standard_normal(int(np.prod(n)))
+        steps = int(rng.integers(0, 9))
+        dt = 0.3 * min(Lj / nj for Lj, nj in zip(L, n))
+        a = port.advect(n, v, L, f0, steps, dt, coeff_form=1)
+        for variant in (1, 2):
+            assert np.array_equal(a, acc.advect(variant, n, v, L, f0, steps, dt)), variant
+
+
 def test_python_reference_close_to_cxx_order(port):
     """The reference's Python class multiplies (dt*coeff)*(...) (upwind.py:64);
     the C++ order differs by rounding only."""

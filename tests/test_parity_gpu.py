@@ -57,6 +57,42 @@ def test_golden_fields(fdb, path, arith):
 
 
 @pytest.mark.parametrize("arith", ARITHS)
+@pytest.mark.parametrize("name", ["acc1_16cube_10", "acc2_16cube_10", "acc2_7x5x6_mixed",
+                                  "python_12cube_10"])
+def test_product_coefficient_form_golden(fdb, name, arith):
+    """The reference variants that round the coefficient as dt * (v*up/dx):
+    upwindAcc.cxx (one advect(dt) call per step), upwindAcc2.cxx and the
+    Python class (upwind.py:32,64).  Under coeff_form="python" EXACT is
+    bit-identical to each; the other arithmetics within 1e-13."""
+    g = load_golden(name)
+    n = [int(x) for x in g["n"]]
+    v = g["v"] if "v" in g else np.ones(3)
+    L = g["L"] if "L" in g else np.ones(3)
+    up = fdb.Upwind(v, L, n, arith="auto", coeff_form="python")
+
+    def go():
+        up.set_arith(arith)
+        if "f0" in g:
+            up.f = g["f0"]
+        if name.startswith("acc1") or name.startswith("python"):
+            for _ in range(int(g["steps"])):  # one advect(dt) per step, as those callers do
+                up.advect(float(g["dt"]))
+        else:
+            up.advect(int(g["steps"]), float(g["dt"]))
+        return up.f, up.checksum(), up.arith_used
+
+    try:
+        out, cs, used = fixed_or_skip(fdb, arith, go)
+    finally:
+        up.close()
+    if used == "exact":
+        assert np.array_equal(out, g["fT"]), rel_maxnorm(out, g["fT"])
+    else:
+        assert rel_maxnorm(out, g["fT"]) <= FIELD_TOL
+    assert cs == pytest.approx(float(g["checksum"]), rel=SUM_TOL)
+
+
+@pytest.mark.parametrize("arith", ARITHS)
 def test_reference_driver_default_128(fdb, arith):
     """The reference driver's configuration (upwind.cxx:174-199): the
     constructor's corner field, v = 1, courant 0.1, 128^3 x 10 steps."""
