@@ -562,6 +562,56 @@ def bench_config(ws: int) -> dict:
             "parallelism": f"replicas x{ws}"}
 
 
+SHARD_PLANES = 512  # planes of axis 0 per rank in the sharded leg (weak scaling)
+
+
+def bench_sharded(steps: int, warmup: int, ws: int) -> dict:
+    """The distributed form (fidibench_gb300.distributed.DistributedUpwind):
+    every rank owns a 512-plane slab of a (512 N) x 512 x 512 periodic grid
+    (N = ranks: the headline workload per rank), v and dt of the headline,
+    100 steps per advect, the K = 3 upwind halo planes exchanged every 3
+    steps (NCCL send/recv between ranks; a device copy of the slab's own far
+    end at N = 1).  Rates over all ranks, timed as the slowest rank."""
+    import torch
+    import fidibench_gb300 as fdb
+    from fidibench_gb300.distributed import DistributedUpwind
+    from fidibench_gb300.sharding import reduce_max
+
+    n = (SHARD_PLANES * ws, N_AXIS, N_AXIS)
+    d = DistributedUpwind(VELOCITY, LENGTHS, n, halo=3)
+    # each rank's slab starts from the headline's initial field
+    src = fdb.Upwind(VELOCITY, LENGTHS, (SHARD_PLANES, N_AXIS, N_AXIS))
+    src.init_sphere(CENTER, RADIUS, NOISE, SEED)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    f = torch.empty(SHARD_PLANES * N_AXIS * N_AXIS, dtype=torch.float64, device=dev)
+    src.get_field(f)
+    src.close()
+    d.slab.set_own(f)
+    del f
+    cur = torch.cuda.current_stream()
+    for _ in range(warmup):
+        d.advect(TIME_STEPS, DT)
+    cur.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(cur)
+    for _ in range(steps):
+        d.advect(TIME_STEPS, DT)
+    e1.record(cur)
+    e1.synchronize()
+    ms = reduce_max(e0.elapsed_time(e1) / steps)
+    cs = d.checksum()
+    used = d.slab.arith_used
+    d.close()
+    cells = float(SHARD_PLANES) * N_AXIS * N_AXIS
+    return {"workload": f"sharded_{SHARD_PLANES}x{N_AXIS}x{N_AXIS}_per_rank_{TIME_STEPS}steps",
+            "ranks": ws, "global_shape": list(n), "halo_planes": d.halo,
+            "exchange": "nccl send/recv" if ws > 1 else "device copy (one rank)",
+            "arith": used, "ms_per_advect": ms,
+            "gcups": ws * cells * TIME_STEPS / (ms * 1e-3) / 1e9, "checksum": cs,
+            "scaling": "weak"}
+
+
 def run_reference_arm(args, ws, rank) -> None:
     """The reference's CPU implementation of the path on the host cores: each
     bench step runs advect() over REF_TIME_STEPS_PER_BENCH_STEP of the
@@ -627,6 +677,8 @@ def main() -> None:
     ap.add_argument("--no-f64-paths", action="store_true",
                     help="skip the FP64 (exact/fma) arithmetic figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-looped leg")
+    ap.add_argument("--no-sharded", action="store_true",
+                    help="skip the distributed (slab-sharded) leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-recovery", action="store_true",
                     help="skip the batched adjoint (gradient-descent recovery) leg")
@@ -765,6 +817,10 @@ def main() -> None:
         up.set_arith(args.arith, args.depth)
     up.close()
 
+    sharded = None
+    if not args.no_sharded:
+        sharded = bench_sharded(max(1, min(args.steps, 3)), 1, ws)
+
     batched = None
     if not args.no_batch:
         batched = bench_batched(max(3, min(args.steps, 5)), 3, stream, rank, ws)
@@ -806,6 +862,7 @@ def main() -> None:
             "f64_paths": f64_paths,
             "clocks": clk,
             "gpu_launches": launches,
+            "sharded": sharded,
             "batched": batched,
             "adjoint": adjoint,
             "batched_adjoint_recovery": recovery,

@@ -60,6 +60,11 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_set_velocity": (_int, [_vp, _vp]),
     "fdb_upwind_set_arith": (_int, [_vp, _int, _int]),
     "fdb_upwind_set_coeff_form": (_int, [_vp, _int]),
+    "fdb_upwind_create_slab": (_int, [_int, _vp, _vp, _vp, ctypes.c_uint64,
+                                      ctypes.POINTER(_vp)]),
+    "fdb_upwind_get_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _int]),
+    "fdb_upwind_set_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _int]),
+    "fdb_upwind_checksum_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _dp]),
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),
     "fdb_checksum_noalloc": (_int, [_vp, ctypes.c_uint64, _vp, _vp]),

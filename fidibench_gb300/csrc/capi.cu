@@ -84,13 +84,19 @@ bool fault_injected(const char* kind) {
 }
 
 int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g) {
+  return make_geom_spacing(ndims, v, L, n, n, g);
+}
+
+int make_geom_spacing(int ndims, const double* v, const double* L, const uint64_t* n,
+                      const uint64_t* n_spacing, Geom* g) {
   if (ndims < 1 || ndims > FDB_MAX_DIMS) return fail(FDB_ERR_INVALID, "ndims must be in [1, 8]");
-  if (!v || !L || !n) return fail(FDB_ERR_INVALID, "null velocity/lengths/num_cells");
+  if (!v || !L || !n || !n_spacing) return fail(FDB_ERR_INVALID, "null velocity/lengths/num_cells");
   Geom r;
   r.ndims = ndims;
   r.ntot = 1;
   for (int j = 0; j < ndims; ++j) {
-    if (n[j] == 0) return fail(FDB_ERR_INVALID, "num_cells must be positive on every axis");
+    if (n[j] == 0 || n_spacing[j] == 0)
+      return fail(FDB_ERR_INVALID, "num_cells must be positive on every axis");
     if (!(L[j] > 0.0) || !isfinite(L[j])) return fail(FDB_ERR_INVALID, "lengths must be finite and > 0");
     if (!isfinite(v[j])) return fail(FDB_ERR_INVALID, "velocity must be finite");
     if (r.ntot > (UINT64_MAX / 16) / n[j]) return fail(FDB_ERR_INVALID, "grid too large");
@@ -99,7 +105,8 @@ int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Ge
     r.L[j] = L[j];
     // upwind.cxx:34-36
     r.up[j] = (v[j] < 0.) ? +1 : -1;
-    r.dx[j] = L[j] / (double)n[j];
+    r.dx[j] = L[j] / (double)n_spacing[j];
+    r.nsp[j] = n_spacing[j];
     r.ntot *= n[j];
   }
   r.dimProd[ndims - 1] = 1;
@@ -464,12 +471,16 @@ const char* fdb_version(void) { return "fidibench_gb300 0.1.0 (sm_103a)"; }
 
 uint64_t fdb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
-int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
-                      const uint64_t* num_cells, fdb_upwind** out) {
+}  // extern "C"
+
+namespace {
+
+int create_handle(int ndims, const double* velocity, const double* lengths,
+                  const uint64_t* num_cells, const uint64_t* n_spacing, fdb_upwind** out) {
   if (!out) return fail(FDB_ERR_INVALID, "null output handle pointer");
   *out = nullptr;
   Geom g;
-  FDB_TRY(make_geom(ndims, velocity, lengths, num_cells, &g));
+  FDB_TRY(make_geom_spacing(ndims, velocity, lengths, num_cells, n_spacing, &g));
   fdb_upwind* h = new fdb_upwind();
   h->g = g;
   int rc = FDB_OK;
@@ -503,6 +514,81 @@ int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
     return rc;
   }
   *out = h;
+  return FDB_OK;
+}
+
+// A plane range [first, first + count) of axis 0, as offsets in values.
+int plane_range(fdb_upwind* h, uint64_t first, uint64_t count, uint64_t* off, uint64_t* len) {
+  const uint64_t plane = h->g.ntot / h->g.n[0];
+  if (first > h->g.n[0] || count > h->g.n[0] - first)
+    return fail(FDB_ERR_INVALID, "plane range outside the field");
+  *off = first * plane;
+  *len = count * plane;
+  return FDB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdb_upwind_create(int ndims, const double* velocity, const double* lengths,
+                      const uint64_t* num_cells, fdb_upwind** out) {
+  return create_handle(ndims, velocity, lengths, num_cells, num_cells, out);
+}
+
+int fdb_upwind_create_slab(int ndims, const double* velocity, const double* lengths,
+                           const uint64_t* num_cells_global, uint64_t slab_planes,
+                           fdb_upwind** out) {
+  if (!num_cells_global) return fail(FDB_ERR_INVALID, "null num_cells_global");
+  if (ndims < 1 || ndims > FDB_MAX_DIMS) return fail(FDB_ERR_INVALID, "ndims must be in [1, 8]");
+  if (slab_planes == 0) return fail(FDB_ERR_INVALID, "slab_planes must be positive");
+  uint64_t n[FDB_MAX_DIMS];
+  for (int j = 0; j < ndims; ++j) n[j] = num_cells_global[j];
+  n[0] = slab_planes;
+  return create_handle(ndims, velocity, lengths, n, num_cells_global, out);
+}
+
+int fdb_upwind_get_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* dst,
+                          int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!dst) return fail(FDB_ERR_INVALID, "null destination");
+  uint64_t off = 0, len = 0;
+  FDB_TRY(plane_range(h, first, count, &off, &len));
+  if (len == 0) return FDB_OK;
+  FDB_CUDA_TRY(cudaMemcpyAsync(dst, h->buf[h->cur] + off, len * sizeof(double),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  return is_device ? FDB_OK : sync(h);
+}
+
+int fdb_upwind_set_planes(fdb_upwind* h, uint64_t first, uint64_t count, const double* src,
+                          int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!src) return fail(FDB_ERR_INVALID, "null source");
+  uint64_t off = 0, len = 0;
+  FDB_TRY(plane_range(h, first, count, &off, &len));
+  h->scale_slot = -1;  // new values: the fixed path measures max|f| again
+  if (len == 0) return FDB_OK;
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->buf[h->cur] + off, src, len * sizeof(double),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               h->stream));
+  return is_device ? FDB_OK : sync(h);
+}
+
+int fdb_upwind_checksum_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* out) {
+  FDB_TRY(check_handle(h));
+  if (!out) return fail(FDB_ERR_INVALID, "null output");
+  uint64_t off = 0, len = 0;
+  FDB_TRY(plane_range(h, first, count, &off, &len));
+  if (len == 0) {
+    *out = 0.0;
+    return FDB_OK;
+  }
+  FDB_TRY(launch_sum(h->buf[h->cur] + off, len, h->part, h->dscal, h->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FDB_TRY(sync(h));
+  *out = h->hscal[0];
   return FDB_OK;
 }
 
@@ -653,7 +739,7 @@ int fdb_upwind_set_velocity(fdb_upwind* h, const double* velocity) {
   FDB_TRY(check_handle(h));
   if (!velocity) return fail(FDB_ERR_INVALID, "null velocity");
   Geom g;
-  FDB_TRY(make_geom(h->g.ndims, velocity, h->g.L, h->g.n, &g));
+  FDB_TRY(make_geom_spacing(h->g.ndims, velocity, h->g.L, h->g.n, h->g.nsp, &g));
   g.coeff_form = h->g.coeff_form;
   h->g = g;
   return FDB_OK;

@@ -84,6 +84,7 @@ struct Geom {
   double dx[FDB_MAX_DIMS] = {0};
   int up[FDB_MAX_DIMS] = {0};
   uint64_t dimProd[FDB_MAX_DIMS] = {0};
+  uint64_t nsp[FDB_MAX_DIMS] = {0};  // the grid the spacings come from (n, or a slab's global grid)
   uint64_t ntot = 0;
   // 3-D view (valid when ndims <= 3)
   int64_t nz = 1, ny = 1, nx = 1;
@@ -93,6 +94,10 @@ struct Geom {
 };
 
 int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g);
+// As make_geom, with the spacings dx_j = L_j / n_spacing[j] of another grid
+// (a slab of a larger grid keeps the global grid's spacings).
+int make_geom_spacing(int ndims, const double* v, const double* L, const uint64_t* n,
+                      const uint64_t* n_spacing, Geom* g);
 
 // The reference coefficient of axis j: ((dt * v_j) * up_j) / dx_j (upwind.cxx:72),
 // or dt * ((v_j * up_j) / dx_j) under FDB_COEFF_PRODUCT (upwindAcc.cxx:45,79).

@@ -109,6 +109,43 @@ int fdb_upwind_advect_host_stream(fdb_upwind* h, int count, const double* const*
                                   double* const* out, int num_steps, double dt,
                                   double* checksums);
 
+/* ---------------------------------------------------------------------------
+ * Slabs of a distributed grid.  The reference distributes its upwind run with
+ * the MPI Filter (upwind/cxx/upwindMpi.cxx:30-165): each rank owns a
+ * sub-domain of CubeDecomp (cxx/CubeDecomp.cpp, Filter.cpp:26-56), fetches the
+ * neighbour's halo window with MPI_Get (Filter.cpp:114-129) before each
+ * stencil term (:212-221) and reduces the checksum with MPI_Reduce (:465-485).
+ * Here a rank owns a slab of consecutive planes of axis 0 (the slowest axis,
+ * so every plane range is one contiguous block), and the halo is the K
+ * planes on the upwind side, exchanged once every K steps
+ * (fidibench_gb300/distributed.py).
+ *
+ * fdb_upwind_create_slab: a handle over slab_planes consecutive planes of
+ * axis 0 of the global grid num_cells_global (other axes whole).  The step
+ * uses the global grid's spacings dx_j = L_j / num_cells_global[j], so its
+ * coefficients are the global problem's bit for bit.  Axis 0 of the slab is
+ * treated as periodic: after k steps the k planes nearest the slab's upwind
+ * end are stale (they read the far end), every other plane is exact.  The
+ * constructor's field is f = 0, f[0] = 1, as for fdb_upwind_create. */
+int fdb_upwind_create_slab(int ndims, const double* velocity, const double* lengths,
+                           const uint64_t* num_cells_global, uint64_t slab_planes,
+                           fdb_upwind** out);
+
+/* Copy planes [first, first + count) of axis 0 of the field out of / into
+ * dst / src.  With is_device = 1 the copy is enqueued on the handle's stream
+ * and not synchronised (order other streams' use of the buffer with events or
+ * by sharing the stream); with host memory the call synchronises.  Works on
+ * any handle; for a slab these are its halo and boundary planes. */
+int fdb_upwind_get_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* dst,
+                          int is_device);
+int fdb_upwind_set_planes(fdb_upwind* h, uint64_t first, uint64_t count, const double* src,
+                          int is_device);
+
+/* checksum() of planes [first, first + count) of axis 0 only (a slab's own
+ * planes, without its halo): the local sum of Filter::computeCheckSum
+ * (Filter.cpp:465-482); the caller reduces over ranks.  Synchronises. */
+int fdb_upwind_checksum_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* out);
+
 /* Replaces std() -- upwind.cxx:95-103 (population standard deviation). */
 int fdb_upwind_std(fdb_upwind* h, double* out);
 

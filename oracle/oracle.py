@@ -71,6 +71,10 @@ class Port:
                                          ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_int]
         lib.fdbo_advect_form.restype = ctypes.c_int
+        lib.fdbo_advect_spacing.argtypes = [ctypes.c_int, _u64p, _dp, _dp, _u64p, _dp, _dp,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_int]
+        lib.fdbo_advect_spacing.restype = ctypes.c_int
         lib.fdbo_checksum.argtypes = [_dp, ctypes.c_uint64]
         lib.fdbo_checksum.restype = ctypes.c_double
         lib.fdbo_std.argtypes = [_dp, ctypes.c_uint64]
@@ -110,6 +114,20 @@ class Port:
         if rc:
             raise ValueError("oracle advect rejected its arguments")
         return f, el
+
+    def advect_spacing(self, n, v, L, n_spacing, f0, steps: int, dt: float,
+                       coeff_form: int = 0) -> np.ndarray:
+        """advect on the grid n with the spacings L_j / n_spacing[j] of
+        another grid (a slab of planes of a larger periodic grid)."""
+        n, v, L, ns = _u64(n), _f64(v), _f64(L), _u64(n_spacing)
+        f = np.array(f0, dtype=np.float64, copy=True).reshape(-1)
+        scratch = np.zeros_like(f)
+        rc = self.lib.fdbo_advect_spacing(len(n), n.ctypes.data_as(_u64p), _ptr(v), _ptr(L),
+                                          ns.ctypes.data_as(_u64p), _ptr(f), _ptr(scratch),
+                                          int(steps), float(dt), 0, int(coeff_form))
+        if rc:
+            raise ValueError("oracle advect rejected its arguments")
+        return f
 
     def checksum(self, f) -> float:
         f = _f64(f).reshape(-1)

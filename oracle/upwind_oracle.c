@@ -49,9 +49,18 @@ typedef struct {
   uint64_t ntot;
 } fdbo_geom;
 
-/* upwind.cxx:27-44 */
+/* upwind.cxx:27-44; the spacings come from the grid n_spacing (n itself,
+ * or the global grid of which n is a slab). */
+static int fdbo_geometry_spacing(int ndims, const uint64_t *n, const double *v,
+                                 const double *L, const uint64_t *n_spacing, fdbo_geom *g);
+
 static int fdbo_geometry(int ndims, const uint64_t *n, const double *v,
                          const double *L, fdbo_geom *g) {
+  return fdbo_geometry_spacing(ndims, n, v, L, n, g);
+}
+
+static int fdbo_geometry_spacing(int ndims, const uint64_t *n, const double *v,
+                                 const double *L, const uint64_t *n_spacing, fdbo_geom *g) {
   if (ndims < 1 || ndims > FDBO_MAXD) return 1;
   g->ndims = ndims;
   g->ntot = 1;
@@ -61,7 +70,8 @@ static int fdbo_geometry(int ndims, const uint64_t *n, const double *v,
     g->v[j] = v[j];
     g->up[j] = -1;
     if (v[j] < 0.) g->up[j] = +1;
-    g->deltas[j] = L[j] / (double)n[j];
+    if (n_spacing[j] == 0) return 1;
+    g->deltas[j] = L[j] / (double)n_spacing[j];
     g->ntot *= n[j];
   }
   g->dimProd[ndims - 1] = 1;
@@ -109,11 +119,31 @@ int fdbo_advect(int ndims, const uint64_t *n, const double *v, const double *L,
   return fdbo_advect_form(ndims, n, v, L, f, oldF, numTimeSteps, deltaTime, nthreads, 0);
 }
 
+static int fdbo_advect_geom(const fdbo_geom *gp, double *f, double *oldF, int numTimeSteps,
+                            double deltaTime, int nthreads, int form);
+
 int fdbo_advect_form(int ndims, const uint64_t *n, const double *v, const double *L,
                      double *f, double *oldF, int numTimeSteps, double deltaTime,
                      int nthreads, int form) {
   fdbo_geom g;
   if (fdbo_geometry(ndims, n, v, L, &g)) return 1;
+  return fdbo_advect_geom(&g, f, oldF, numTimeSteps, deltaTime, nthreads, form);
+}
+
+/* advect on a grid n whose spacings are those of the grid n_spacing (a slab
+ * of planes of axis 0 of a larger periodic grid, treated as periodic itself:
+ * the test harness of the distributed form). */
+int fdbo_advect_spacing(int ndims, const uint64_t *n, const double *v, const double *L,
+                        const uint64_t *n_spacing, double *f, double *oldF, int numTimeSteps,
+                        double deltaTime, int nthreads, int form) {
+  fdbo_geom g;
+  if (fdbo_geometry_spacing(ndims, n, v, L, n_spacing, &g)) return 1;
+  return fdbo_advect_geom(&g, f, oldF, numTimeSteps, deltaTime, nthreads, form);
+}
+
+static int fdbo_advect_geom(const fdbo_geom *gp, double *f, double *oldF, int numTimeSteps,
+                            double deltaTime, int nthreads, int form) {
+  const fdbo_geom g = *gp;
   const int64_t ntot = (int64_t)g.ntot;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
