@@ -587,8 +587,9 @@ def bench_sharded(steps: int, warmup: int, ws: int) -> dict:
     src.get_field(f)
     src.close()
     d.slab.set_own(f)
+    d.stream.synchronize()  # the copy out of f ends before f is freed
     del f
-    cur = torch.cuda.current_stream()
+    cur = d.stream  # the slab's stream: its copies, transfers and steps
     for _ in range(warmup):
         d.advect(TIME_STEPS, DT)
     cur.synchronize()

@@ -25,7 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_lib", "obj")
 LIB = os.path.join(PKG, "_lib", "libfdb_upwind.so")
 DRIVER = os.path.join(PKG, "_lib", "upwindCxx")
-DRIVERS = ("upwindCxx", "upwindAccCxx", "upwindAcc2Cxx", "laplacian")  # drivers/<name>.cpp -> _lib/<name>
+DRIVERS = ("upwindCxx", "upwindAccCxx", "upwindAcc2Cxx", "upwindMpiCxx", "laplacian", "testStencil2d")  # drivers/<name>.cpp -> _lib/<name>
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -143,7 +143,12 @@ class UpwindSlab:
     def set_own(self, values) -> None:
         first, count = self.layout.own
         if getattr(values, "is_cuda", False):
-            self.set_planes(first, count, values.contiguous())
+            import torch
+            t = values.contiguous()
+            if t.numel() != count * self.plane:
+                raise ValueError(f"slab has {count * self.plane} values, got {t.numel()}")
+            torch.cuda.current_stream(t.device).synchronize()  # written on torch's stream
+            self.set_planes(first, count, t)
         else:
             a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
             if a.size != count * self.plane:
@@ -184,8 +189,9 @@ class DistributedUpwind:
     group when initialised, else one rank).  halo: steps between exchanges
     (capped by the thinnest slab).  slab_factory: callable(SlabLayout) ->
     slab object (tests put a CPU stand-in here); default an UpwindSlab on the
-    current GPU enqueuing on torch's current stream, so that NCCL transfers
-    order with it."""
+    current GPU.  The GPU slab enqueues on its own torch stream (`stream`),
+    and the NCCL transfers are issued with that stream current, so copies,
+    transfers and steps are ordered on the device without host waits."""
 
     def __init__(self, velocity, lengths, numCells, group=None, halo: int = 3,
                  arith: str = "auto", depth: int = 0, coeff_form: str = "cxx",
@@ -208,10 +214,12 @@ class DistributedUpwind:
         # device buffers for NCCL and for the single-rank self-exchange on the
         # GPU; host buffers for gloo (and for CPU stand-in slabs)
         self.on_device = self.backend == "nccl" or (self.world == 1 and slab_factory is None)
+        self.stream = None
         if slab_factory is None:
             slab = UpwindSlab(velocity, lengths, self.numCells, self.layout, arith, depth,
                               coeff_form)
-            slab.set_stream(torch.cuda.current_stream())
+            self.stream = torch.cuda.Stream()
+            slab.set_stream(self.stream)
         else:
             slab = slab_factory(self.layout)
         self.slab = slab
@@ -247,10 +255,16 @@ class DistributedUpwind:
         hmax = max(z1 - z0 for z0, z1 in self.bounds)
         pad = np.zeros(hmax * self.plane)
         pad[:own.size] = own
-        dev = torch.device("cuda", torch.cuda.current_device()) if self.on_device else "cpu"
-        t = torch.from_numpy(pad).to(dev)
-        parts = [torch.empty_like(t) for _ in range(self.world)]
-        dist.all_gather(parts, t, group=self.group)
+        if self.on_device:
+            with torch.cuda.stream(self.stream):
+                t = torch.from_numpy(pad).to(torch.device("cuda", torch.cuda.current_device()))
+                parts = [torch.empty_like(t) for _ in range(self.world)]
+                dist.all_gather(parts, t, group=self.group)
+                self.stream.synchronize()
+        else:
+            t = torch.from_numpy(pad)
+            parts = [torch.empty_like(t) for _ in range(self.world)]
+            dist.all_gather(parts, t, group=self.group)
         return np.concatenate([parts[r].cpu().numpy()[:(z1 - z0) * self.plane]
                                for r, (z0, z1) in enumerate(self.bounds)])
 
@@ -265,8 +279,15 @@ class DistributedUpwind:
             return
         ops = [dist.P2POp(dist.isend, self._send, lay.downwind, self.group),
                dist.P2POp(dist.irecv, self._recv, lay.upwind, self.group)]
-        for req in dist.batch_isend_irecv(ops):
-            req.wait()
+        if self.on_device:
+            import torch
+            # NCCL waits for, and is waited on by, the current stream: the slab's
+            with torch.cuda.stream(self.stream):
+                for req in dist.batch_isend_irecv(ops):
+                    req.wait()
+        else:
+            for req in dist.batch_isend_irecv(ops):
+                req.wait()
         self.slab.set_planes(lay.halo_at[0], lay.halo_at[1], self._recv)
 
     def advect(self, numTimeSteps: int, deltaTime: float) -> None:
@@ -284,8 +305,13 @@ class DistributedUpwind:
         local = float(self.slab.checksum_own())
         if self.world == 1:
             return local
-        dev = torch.device("cuda", torch.cuda.current_device()) if self.on_device else "cpu"
-        t = torch.tensor([local], dtype=torch.float64, device=dev)
+        if self.on_device:
+            with torch.cuda.stream(self.stream):
+                t = torch.tensor([local], dtype=torch.float64,
+                                 device=torch.device("cuda", torch.cuda.current_device()))
+                dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)
+                return float(t.item())
+        t = torch.tensor([local], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)
         return float(t.item())
 
@@ -293,8 +319,8 @@ class DistributedUpwind:
 class SlabRing:
     """Every slab of a `world`-way decomposition in this process, on the
     current GPU: the exchange of DistributedUpwind with device copies between
-    the slabs' buffers in place of sends.  All slabs share torch's current
-    stream, so the copies and the steps are ordered."""
+    the slabs' buffers in place of sends.  All slabs enqueue on one torch
+    stream (`stream`), so the copies and the steps are ordered."""
 
     def __init__(self, velocity, lengths, numCells, world: int, halo: int = 3,
                  arith: str = "auto", depth: int = 0, coeff_form: str = "cxx"):
@@ -307,10 +333,10 @@ class SlabRing:
         self.layouts = [SlabLayout(z0, z1, self.halo, float(velocity[0]), world, r)
                         for r, (z0, z1) in enumerate(self.bounds)]
         self.slabs = []
-        stream = torch.cuda.current_stream()
+        self.stream = torch.cuda.Stream()
         for lay in self.layouts:
             s = UpwindSlab(velocity, lengths, self.numCells, lay, arith, depth, coeff_form)
-            s.set_stream(stream)
+            s.set_stream(self.stream)
             self.slabs.append(s)
         dev = torch.device("cuda", torch.cuda.current_device())
         self._tmp = [torch.empty(self.halo * self.plane, dtype=torch.float64, device=dev)

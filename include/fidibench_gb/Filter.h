@@ -28,15 +28,24 @@
 #ifndef FIDIBENCH_GB_FILTER_H
 #define FIDIBENCH_GB_FILTER_H
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
+#include <functional>
 #include <iostream>
+#include <limits>
 #include <map>
+#include <numeric>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
+// (the standard headers the reference's Filter.h brings in through
+// CubeDecomp.h, MultiArrayIter.h and writeVTK.h, so that drivers relying on
+// them -- upwindMpi.cxx uses std::accumulate -- compile unchanged)
 
 #include "../fdb_filter.h"
 #include "../fdb_upwind.h"

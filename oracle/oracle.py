@@ -20,6 +20,7 @@ PORT_SO = os.path.join(HERE, "_build", "libfdb_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfdb_refupwind.so")
 REF_EXE = os.path.join(HERE, "_ref", "upwindCxx")
 REF_ACC_SO = os.path.join(HERE, "_ref", "libfdb_refacc.so")
+REF_FILTER_SO = os.path.join(HERE, "_ref", "libfdb_reffilter.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -309,6 +310,44 @@ class ReferenceAcc:
         if rc:
             raise ValueError("reference OpenACC harness rejected its arguments")
         return out
+
+
+class ReferenceFilter:
+    """The reference's stencil Filter (cxx/Filter.cpp and its CubeDecomp,
+    MultiArrayIter, writeVTK) for one rank on oracle/mpi_stub, compiled by
+    ref_filter_harness.cpp, when built here."""
+
+    def __init__(self, path: str = REF_FILTER_SO):
+        if not os.path.isfile(path):
+            raise FileNotFoundError(path)
+        lib = ctypes.CDLL(path)
+        _ip = ctypes.POINTER(ctypes.c_int)
+        lib.fdbr_filter_run.argtypes = [ctypes.c_int, _u64p, ctypes.c_int, _ip, _dp, _dp, _dp,
+                                        ctypes.c_int, _dp]
+        lib.fdbr_filter_run.restype = ctypes.c_int
+        self.lib = lib
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.isfile(REF_FILTER_SO)
+
+    def run(self, dims, stencil, f_in, iterations: int = 1):
+        """(outData, (input checksum, output checksum)) after `iterations`
+        applyFilter calls with copyOutToIn between them; `stencil` is a dict
+        or a list of (offset, weight) pairs inserted in order."""
+        items = list(stencil.items()) if hasattr(stencil, "items") else list(stencil)
+        dims = _u64(dims)
+        offs = np.ascontiguousarray(np.array([o for o, _ in items], dtype=np.int32).reshape(-1))
+        w = _f64([x for _, x in items])
+        fi = _f64(f_in).reshape(-1)
+        out = np.empty_like(fi)
+        sums = np.zeros(2)
+        rc = self.lib.fdbr_filter_run(len(dims), dims.ctypes.data_as(_u64p), len(items),
+                                      offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                      _ptr(w), _ptr(fi), _ptr(out), int(iterations), _ptr(sums))
+        if rc:
+            raise ValueError(f"reference Filter harness rejected its arguments ({rc})")
+        return out, (float(sums[0]), float(sums[1]))
 
 
 def reference_dt(n, v, L, courant: float) -> float:

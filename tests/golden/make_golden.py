@@ -124,6 +124,86 @@ def acc_cases(port: Port) -> None:
          checksum=np.float64(port.checksum(fT)))
 
 
+def filter_cases(port: Port) -> None:
+    """The reference's stencil Filter (cxx/Filter.cpp, one rank on
+    oracle/mpi_stub; oracle/ref_filter_harness.cpp): the laplacian driver's
+    stencil (laplacian/cxx/laplacian.cxx:55-65) on sin inputs, 2-D and 3-D, on
+    power-of-two and other grids (the latter exercise the `%= size_t` wrap,
+    Filter.cpp:238-240); testStencil2d.cxx's stencil and input; the upwindMpi
+    stencil (upwind/cxx/upwindMpi.cxx:74-92) with its corner input over 10
+    steps; a seeded general stencil with repeated offsets."""
+    from oracle.oracle import ReferenceFilter
+    flt = ReferenceFilter()
+
+    def lap(nd):
+        st = [(tuple([0] * nd), -2.0 * nd)]
+        for i in range(nd):
+            for s_ in (1, -1):
+                o = [0] * nd
+                o[i] = s_
+                st.append((tuple(o), 1.0))
+        return st
+
+    def store(name, dims, st, f0, iters):
+        out, sums = flt.run(dims, st, f0, iters)
+        save(name, dims=np.asarray(dims, np.uint64),
+             offsets=np.array([o for o, _ in st], np.int32),
+             weights=np.array([w for _, w in st], np.float64), f0=f0, iterations=np.int64(iters),
+             out=out, sums=np.array(sums, np.float64))
+
+    for dims, iters in (((16, 16), 1), ((10, 12), 1), ((6, 5, 7), 1), ((16, 16), 10)):
+        nd = len(dims)
+        f0 = port.filter_sin_input(dims, [0.0] * nd, [1.0] * nd)
+        name = "filter_lap" + "x".join(str(d) for d in dims) + f"_it{iters}"
+        store(name, dims, lap(nd), f0, iters)
+    # testStencil2d.cxx: 1 on the cells with a zero index, stencil
+    # {0: 0, (1, 0): 1, (0, -1): -1}
+    n = 8
+    i, j = np.arange(n * n) % n, np.arange(n * n) // n
+    store("filter_stencil2d_8", (n, n), [((0, 0), 0.0), ((1, 0), 1.0), ((0, -1), -1.0)],
+          ((i * j) == 0).astype(float), 1)
+    # upwindMpi.cxx: v = 1, courant 0.1, N = 16, corner input, 10 steps
+    N = 16
+    dt = 0.1 * (1.0 / N)
+    c = dt * 1.0 / (1.0 / N)
+    diag = 1.0
+    for _ in range(3):
+        diag -= 1 * dt * 1.0 / (1.0 / N)
+    st = [((0, 0, 0), diag), ((-1, 0, 0), c), ((0, -1, 0), c), ((0, 0, -1), c)]
+    f0 = np.zeros(N ** 3)
+    f0[0] = 1.0
+    store("filter_upwindmpi_16_it10", (N, N, N), st, f0, 10)
+    # a general stencil: offsets up to +-2, a repeated offset (first weight wins)
+    rng = np.random.default_rng(SEED + 11)
+    dims = (7, 5, 6)
+    st = [((0, 0, 0), 0.75), ((2, 0, -1), -1.25), ((-1, 1, 0), 0.5), ((0, -2, 2), 2.0),
+          ((2, 0, -1), 9.0), ((1, 1, 1), -0.375)]
+    store("filter_general_7x5x6", dims, st, rng.standard_normal(int(np.prod(dims))), 2)
+
+
+def filter_driver_cases() -> None:
+    """The reference's Filter drivers, built unmodified for one rank on
+    oracle/mpi_stub (oracle/_ref/{laplacian,testStencil2d,upwindMpiCxx}):
+    their output lines (timing lines dropped; testStencil2d prints its
+    outData to stderr)."""
+    import subprocess
+    import tempfile
+    runs = {
+        "laplacian_2d_16": ("laplacian", ["-numCells", "16", "-numDims", "2"]),
+        "laplacian_3d_8": ("laplacian", ["-numCells", "8", "-numDims", "3"]),
+        "teststencil2d_8": ("testStencil2d", ["-numCells", "8"]),
+        "upwindmpi_16_5": ("upwindMpiCxx", ["-numCells", "16", "-numSteps", "5"]),
+    }
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for key, (exe, args) in runs.items():
+            r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", exe)] + args, cwd=d,
+                               capture_output=True, text=True, check=True)
+            lines = [ln for ln in (r.stdout + r.stderr).splitlines() if "times" not in ln]
+            out[key] = np.array("\n".join(lines))
+    save("filterdrivers_stdout", **out)
+
+
 def vtk_case() -> None:
     """The reference driver binary (oracle/_ref/upwindCxx, built from the
     reference's own upwind.cxx + CmdLineArgParser.cpp) with -vtk -std: its
@@ -158,6 +238,8 @@ def main() -> None:
     driver_cases(ref)
     python_reference_case()
     acc_cases(port)
+    filter_cases(port)
+    filter_driver_cases()
     vtk_case()
     synth_case(port)
 

@@ -1,6 +1,10 @@
-"""The stencil Filter's CPU restatement (oracle/filter_oracle.c) against known
-answers read from the reference's sources (cxx/Filter.cpp, laplacian/cxx/):
-the reference's Filter needs MPI, which this image lacks, so it is not run.
+"""The stencil Filter's CPU restatement (oracle/filter_oracle.c), pinned bit
+for bit to the reference's own Filter (cxx/Filter.cpp with CubeDecomp,
+MultiArrayIter and writeVTK), which oracle/Makefile compiles for one rank
+against the single-rank MPI stand-in oracle/mpi_stub: through the golden
+fixtures tests/golden/filter_*.npz that tests/golden/make_golden.py made from
+it, and (where it was built here) against the compiled reference directly on
+seeded random stencils.  Also known answers read from the reference's sources:
 
   * the discrete Laplacian of prod_j sin(2 pi x_j) on a periodic power-of-two
     grid is sum_j 2 (cos(2 pi / N_j) - 1) times the input (to rounding);
@@ -16,6 +20,51 @@ import math
 
 import numpy as np
 import pytest
+
+from conftest import golden_files, load_golden
+
+FILTER_GOLDEN = golden_files("filter_*.npz")
+
+
+def golden_stencil(g):
+    nd = len(g["dims"])
+    offs = [tuple(int(x) for x in o) for o in g["offsets"].reshape(-1, nd)]
+    return list(zip(offs, [float(w) for w in g["weights"]]))
+
+
+@pytest.mark.parametrize("path", FILTER_GOLDEN, ids=lambda p: p.split("/")[-1][:-4])
+def test_port_matches_reference_filter_golden(port, path):
+    g = load_golden(path)
+    dims = [int(x) for x in g["dims"]]
+    st = golden_stencil(g)
+    f = g["f0"]
+    for _ in range(int(g["iterations"])):
+        f = port.filter_apply(dims, st, f)
+    assert np.array_equal(f, g["out"])
+    assert np.array_equal(np.signbit(f), np.signbit(g["out"]))
+    assert port.filter_checksum(f) == float(g["sums"][1])
+
+
+def test_port_matches_compiled_reference_filter(port):
+    from oracle.oracle import ReferenceFilter
+    if not ReferenceFilter.available():
+        pytest.skip("reference Filter not built in this tree")
+    ref = ReferenceFilter()
+    rng = np.random.default_rng(41)
+    for _ in range(10):
+        nd = int(rng.integers(1, 4))
+        dims = [int(x) for x in rng.integers(2, 9, size=nd)]
+        nt = int(rng.integers(1, 6))
+        st = [(tuple(int(x) for x in rng.integers(-2, 3, size=nd)), float(rng.normal()))
+              for _ in range(nt)]
+        f0 = rng.standard_normal(int(np.prod(dims)))
+        iters = int(rng.integers(1, 4))
+        out, sums = ref.run(dims, st, f0, iters)
+        f = f0
+        for _ in range(iters):
+            f = port.filter_apply(dims, st, f)
+        assert np.array_equal(f, out), (dims, st)
+        assert port.filter_checksum(f) == sums[1]
 
 
 def laplacian_stencil(nd):

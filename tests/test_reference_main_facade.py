@@ -12,6 +12,12 @@ keep the driver, drop the in-file class, include the facade.
   upwind/cxx/upwindAcc2.cxx  main() (:137-193): std::vector<int> ctor,
                              advect(int, double), std()
 
+The same for the Filter facade (include/fidibench_gb/Filter.h): the
+reference's Filter drivers laplacian/cxx/laplacian.cxx, testStencil2d.cxx and
+upwind/cxx/upwindMpi.cxx, whole and unchanged, with the single-rank MPI
+stand-in oracle/mpi_stub providing MPI_Init, MPI_Wtime, MPI_Reduce and the
+other calls they make outside the Filter.
+
 The built programs run `-h` here (no GPU needed: help only); their numerical
 twins, this repository's drivers, run the ctest cases in the GPU suite.  CPU
 only; skipped where the reference tree is absent."""
@@ -76,6 +82,33 @@ def test_reference_main_builds_against_facade(src, lib_dir, tmp_path):
         ["g++", "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include"),
          "-I", os.path.join(refdir, "cxx"), str(tu),
          os.path.join(refdir, "cxx", "CmdLineArgParser.cpp"), "-o", str(exe),
+         "-L", lib_dir, "-lfdb_upwind", "-Wl,-rpath," + lib_dir],
+        capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-4000:]
+    h = subprocess.run([str(exe), "-h"], capture_output=True, text=True, timeout=60)
+    assert h.returncode == 0, h.stderr
+    assert "-numCells" in h.stdout
+
+
+@pytest.mark.parametrize("src", ["laplacian/cxx/laplacian.cxx", "laplacian/cxx/testStencil2d.cxx",
+                                 "upwind/cxx/upwindMpi.cxx"])
+def test_reference_filter_driver_builds_against_facade(src, lib_dir, tmp_path):
+    refdir = _refdir()
+    path = os.path.join(refdir, src)
+    if not os.path.isfile(path):
+        pytest.skip("the reference source tree is not present")
+    stub = os.path.join(ROOT, "oracle", "mpi_stub")
+    obj = tmp_path / "mpi_stub.o"
+    r = subprocess.run(["gcc", "-std=c11", "-O1", "-D_POSIX_C_SOURCE=199309L", "-I", stub, "-c",
+                        os.path.join(stub, "mpi_stub.c"), "-o", str(obj)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    exe = tmp_path / os.path.basename(src).replace(".cxx", "")
+    # include/fidibench_gb first: the driver's "Filter.h" is the facade
+    r = subprocess.run(
+        ["g++", "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include", "fidibench_gb"),
+         "-I", os.path.join(ROOT, "include"), "-I", stub, "-I", os.path.join(refdir, "cxx"),
+         path, os.path.join(refdir, "cxx", "CmdLineArgParser.cpp"), str(obj), "-o", str(exe),
          "-L", lib_dir, "-lfdb_upwind", "-Wl,-rpath," + lib_dir],
         capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-4000:]
