@@ -65,6 +65,11 @@ SIGNATURES: dict[str, tuple] = {
     "fdb_upwind_get_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _int]),
     "fdb_upwind_set_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _int]),
     "fdb_upwind_checksum_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _dp]),
+    "fdb_upwind_set_own_planes": (_int, [_vp, ctypes.c_uint64, ctypes.c_uint64]),
+    "fdb_upwind_block_begin": (_int, [_vp, ctypes.c_double, ctypes.POINTER(_int)]),
+    "fdb_upwind_advect_block": (_int, [_vp, _int, ctypes.c_double, _int]),
+    "fdb_upwind_get_scale_word": (_int, [_vp, _vp, _int]),
+    "fdb_upwind_set_scale_word": (_int, [_vp, _vp, _int]),
     "fdb_upwind_info": (_int, [_vp, _u64p, ctypes.POINTER(_int)]),
     "fdb_upwind_set_tuning": (_int, [_vp, _int, _int]),
     "fdb_checksum_noalloc": (_int, [_vp, ctypes.c_uint64, _vp, _vp]),

@@ -56,6 +56,14 @@ struct fdb_upwind {
   fdb::DeviceScratch contract;  // the closed form's contraction tables and partials
   cudaStream_t io_stream[2] = {nullptr, nullptr};
   cudaEvent_t io_ev[7] = {};
+  // an open block chain (fdb_upwind_block_begin .. the last
+  // fdb_upwind_advect_block): arithmetic, ring position of the next launch,
+  // whether it reads FP64, and the depth its guard bits are sized for
+  int chain = 0;
+  int chain_arith = 0;
+  int chain_i = 0;
+  int chain_first = 0;
+  int chain_K = 0;
 };
 
 namespace fdb {
@@ -160,6 +168,16 @@ namespace {
 
 int check_handle(fdb_upwind* h) {
   if (!h) return fail(FDB_ERR_INVALID, "null handle");
+  return FDB_OK;
+}
+
+// Calls that read, write or advance the field as FP64 need it closed: between
+// fdb_upwind_block_begin and the last block the buffers may hold int64.
+int check_no_chain(fdb_upwind* h) {
+  FDB_TRY(check_handle(h));
+  if (h->chain)
+    return fail(FDB_ERR_INVALID, "a block chain is open (finish it with a last "
+                                 "fdb_upwind_advect_block first)");
   return FDB_OK;
 }
 
@@ -567,7 +585,9 @@ int fdb_upwind_set_planes(fdb_upwind* h, uint64_t first, uint64_t count, const d
   if (!src) return fail(FDB_ERR_INVALID, "null source");
   uint64_t off = 0, len = 0;
   FDB_TRY(plane_range(h, first, count, &off, &len));
-  h->scale_slot = -1;  // new values: the fixed path measures max|f| again
+  // new values: the fixed path measures max|f| again (inside a block chain
+  // the caller agrees the scale word instead)
+  if (!h->chain) h->scale_slot = -1;
   if (len == 0) return FDB_OK;
   FDB_CUDA_TRY(cudaMemcpyAsync(h->buf[h->cur] + off, src, len * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
@@ -575,8 +595,91 @@ int fdb_upwind_set_planes(fdb_upwind* h, uint64_t first, uint64_t count, const d
   return is_device ? FDB_OK : sync(h);
 }
 
-int fdb_upwind_checksum_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* out) {
+int fdb_upwind_set_own_planes(fdb_upwind* h, uint64_t first, uint64_t count) {
+  FDB_TRY(check_no_chain(h));
+  if (count == 0 || first > h->g.n[0] || count > h->g.n[0] - first)
+    return fail(FDB_ERR_INVALID, "own planes outside the field");
+  h->g.own0 = first;
+  h->g.own_n = count == h->g.n[0] ? 0 : count;
+  h->scale_slot = -1;
+  return FDB_OK;
+}
+
+int fdb_upwind_block_begin(fdb_upwind* h, double dt, int* fixed) {
+  FDB_TRY(check_no_chain(h));
+  if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
+  int arith = 0;
+  FDB_TRY(pick_arith(h, dt, &arith));
+  h->arith_used = arith;
+  h->chain_arith = arith;
+  h->chain_first = 1;
+  if (arith == FDB_ARITH_FIXED) {
+    h->chain_K = h->depth > 0 ? h->depth : default_depth(h->g);
+    if (h->scale_slot < 0) {
+      FDB_TRY(launch_scale_prepass(h->g, h->buf[h->cur], h->scratch, h->stream));
+      h->scale_slot = 0;
+    }
+    h->chain_i = h->scale_slot;
+  }
+  h->chain = 1;
+  if (fixed) *fixed = arith == FDB_ARITH_FIXED;
+  return FDB_OK;
+}
+
+int fdb_upwind_advect_block(fdb_upwind* h, int steps, double dt, int last) {
+  NvtxScope nvtx_("fdb.advect_block");
   FDB_TRY(check_handle(h));
+  if (!h->chain) return fail(FDB_ERR_INVALID, "no block chain is open (fdb_upwind_block_begin)");
+  if (steps < 1) return fail(FDB_ERR_INVALID, "a block advances at least one step");
+  if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
+  const Coeffs3 c = coeffs3(h->g, dt);
+  int rc = FDB_OK;
+  if (h->chain_arith == FDB_ARITH_FIXED) {
+    if (steps > h->chain_K)
+      return fail(FDB_ERR_INVALID, "a fixed-point block advances at most its depth of steps");
+    rc = launch_fixed_block(h->g, c, steps, h->tune, h->chain_K, h->buf, &h->cur,
+                            h->chain_first != 0, last != 0, h->scratch, h->chain_i, h->stream);
+    if (!rc) {
+      ++h->chain_i;
+      h->chain_first = 0;
+      if (last) h->scale_slot = h->chain_i % 3;
+    }
+  } else {
+    rc = advance(h, steps, dt, h->chain_arith);
+  }
+  if (rc) {
+    h->chain = 0;  // the field is no longer defined: measure afresh next time
+    h->scale_slot = -1;
+    return rc;
+  }
+  if (last) h->chain = 0;
+  return FDB_OK;
+}
+
+int fdb_upwind_get_scale_word(fdb_upwind* h, uint64_t* dst, int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!dst) return fail(FDB_ERR_INVALID, "null destination");
+  if (!h->chain || h->chain_arith != FDB_ARITH_FIXED)
+    return fail(FDB_ERR_INVALID, "no fixed-point block chain is open");
+  FDB_CUDA_TRY(cudaMemcpyAsync(dst, scale_word(h->scratch, h->chain_i), sizeof(uint64_t),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+  return is_device ? FDB_OK : sync(h);
+}
+
+int fdb_upwind_set_scale_word(fdb_upwind* h, const uint64_t* src, int is_device) {
+  FDB_TRY(check_handle(h));
+  if (!src) return fail(FDB_ERR_INVALID, "null source");
+  if (!h->chain || h->chain_arith != FDB_ARITH_FIXED)
+    return fail(FDB_ERR_INVALID, "no fixed-point block chain is open");
+  FDB_CUDA_TRY(cudaMemcpyAsync(scale_word(h->scratch, h->chain_i), src, sizeof(uint64_t),
+                               is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               h->stream));
+  return is_device ? FDB_OK : sync(h);
+}
+
+int fdb_upwind_checksum_planes(fdb_upwind* h, uint64_t first, uint64_t count, double* out) {
+  FDB_TRY(check_no_chain(h));
   if (!out) return fail(FDB_ERR_INVALID, "null output");
   uint64_t off = 0, len = 0;
   FDB_TRY(plane_range(h, first, count, &off, &len));
@@ -616,7 +719,7 @@ int fdb_upwind_destroy(fdb_upwind* h) {
 }
 
 int fdb_upwind_set_field(fdb_upwind* h, const double* src, int is_device) {
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (!src) return fail(FDB_ERR_INVALID, "null source field");
   h->scale_slot = -1;
   FDB_CUDA_TRY(cudaMemcpyAsync(h->buf[h->cur], src, h->g.ntot * sizeof(double),
@@ -626,7 +729,7 @@ int fdb_upwind_set_field(fdb_upwind* h, const double* src, int is_device) {
 }
 
 int fdb_upwind_get_field(fdb_upwind* h, double* dst, int is_device) {
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (!dst) return fail(FDB_ERR_INVALID, "null destination field");
   FDB_CUDA_TRY(cudaMemcpyAsync(dst, h->buf[h->cur], h->g.ntot * sizeof(double),
                                is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
@@ -644,7 +747,7 @@ int fdb_upwind_field_ptr(fdb_upwind* h, double** out) {
 
 int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt) {
   NvtxScope nvtx_("fdb.advect");
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
   if (num_steps == 0) return FDB_OK;
@@ -655,7 +758,7 @@ int fdb_upwind_advect(fdb_upwind* h, int num_steps, double dt) {
 }
 
 int fdb_upwind_checksum(fdb_upwind* h, double* out) {
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (!out) return fail(FDB_ERR_INVALID, "null output");
   FDB_TRY(launch_sum(h->buf[h->cur], h->g.ntot, h->part, h->dscal, h->stream));
   FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost,
@@ -669,7 +772,7 @@ int fdb_upwind_advect_host_stream(fdb_upwind* h, int count, const double* const*
                                   double* const* out, int num_steps, double dt,
                                   double* checksums) {
   NvtxScope nvtx_("fdb.advect_host_stream");
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (count < 0) return fail(FDB_ERR_INVALID, "count must be >= 0");
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
@@ -715,7 +818,7 @@ int fdb_upwind_advect_host_stream(fdb_upwind* h, int count, const double* const*
 int fdb_upwind_advect_transposed(fdb_upwind* h, int num_steps, double dt, const double* in,
                                  double* out, int is_device) {
   NvtxScope nvtx_("fdb.advect_transposed");
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (h->g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "the transposed advect serves ndims <= 3");
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");
   if (!isfinite(dt)) return fail(FDB_ERR_INVALID, "dt must be finite");
@@ -725,7 +828,7 @@ int fdb_upwind_advect_transposed(fdb_upwind* h, int num_steps, double dt, const 
 }
 
 int fdb_upwind_std(fdb_upwind* h, double* out) {
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (!out) return fail(FDB_ERR_INVALID, "null output");
   FDB_TRY(launch_std(h->buf[h->cur], h->g.ntot, h->part, h->dscal + 1, h->dscal, h->stream));
   FDB_CUDA_TRY(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost,
@@ -800,7 +903,7 @@ int fdb_upwind_info(fdb_upwind* h, uint64_t* ntot, int* arith_used) {
 
 int fdb_upwind_init_sphere(fdb_upwind* h, const double* center, double radius, double noise_amp,
                            uint64_t seed) {
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   if (!center) return fail(FDB_ERR_INVALID, "null centre");
   h->scale_slot = -1;
   FDB_TRY(launch_sphere_noise(h->g, center, radius, noise_amp, seed, h->buf[h->cur], h->stream));
@@ -838,7 +941,7 @@ int fdb_upwind_adjoint_step(fdb_upwind* h, double dt, const double* f_dev,
 int fdb_upwind_adjoint(fdb_upwind* h, int num_steps, double dt, const double* lambda_T,
                        double* grad_f0, double* grad_v, int checkpoint_every, int is_device) {
   NvtxScope nvtx_("fdb.adjoint");
-  FDB_TRY(check_handle(h));
+  FDB_TRY(check_no_chain(h));
   const Geom& g = h->g;
   if (g.ndims > 3) return fail(FDB_ERR_UNSUPPORTED, "adjoint serves ndims <= 3");
   if (num_steps < 0) return fail(FDB_ERR_INVALID, "num_steps must be >= 0");

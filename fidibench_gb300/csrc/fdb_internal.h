@@ -91,6 +91,10 @@ struct Geom {
   int upz = -1, upy = -1, upx = -1;
   int jz = -1, jy = -1, jx = -1;  // reference axis of each internal axis (-1: padded)
   int coeff_form = FDB_COEFF_CXX;  // how ref_coeff rounds c_j (FDB_COEFF_*)
+  // a slab's own planes [own0, own0 + own_n) of axis 0 (own_n = 0: all): the
+  // fixed-point scale is measured over them only, so that every slab of a
+  // distributed grid can agree on the global one
+  uint64_t own0 = 0, own_n = 0;
 };
 
 int make_geom(int ndims, const double* v, const double* L, const uint64_t* n, Geom* g);
@@ -143,11 +147,25 @@ struct FixedTuning {
 int launch_advect_fixed(const Geom& g, const Coeffs3& c, int steps, int depth,
                         double** buf, int* cur, double* d_scratch, size_t scratch_bytes,
                         cudaStream_t s);
+// The scale pre-pass: slot ring reset, slot 0 = max|f| (FP64 bits) of the
+// geometry's own planes of f.
+int launch_scale_prepass(const Geom& g, const double* f, double* d_scratch, cudaStream_t s);
 // As above; *scale_slot (in/out, may be null) names the scratch slot that
 // holds max|f| of the current field (-1: unknown, a pre-pass measures it).
 int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const FixedTuning& tune,
                            double** buf, int* cur, double* d_scratch, size_t scratch_bytes,
                            int* scale_slot, cudaStream_t s);
+
+// One launch of a block chain (fdb_upwind_advect_block): k <= guard_K steps
+// at ring position i, FP64 in/out as asked, int64 otherwise; flips *cur.
+// The launches of a chain are those launch_advect_fixed_ex makes for the
+// same steps, so the field is the same bit for bit.
+int launch_fixed_block(const Geom& g, const Coeffs3& c, int k, const FixedTuning& tune,
+                       int guard_K, double** buf, int* cur, bool in_f64, bool out_f64,
+                       double* d_scratch, int i, cudaStream_t s);
+// The 64-bit word of ring slot i that the launch at position i reads to set
+// its scale (FP64 bits of max|f| after a pre-pass, else an OR of |F|).
+uint64_t* scale_word(double* d_scratch, int i);
 
 // Deterministic reductions.  `part` holds at least reduce_partials(n) doubles.
 uint32_t reduce_partials(uint64_t n);

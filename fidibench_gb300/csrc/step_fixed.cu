@@ -134,6 +134,15 @@ fx::FixedArgs make_fixed_args(const Geom& g, const Coeffs3& c, int shape, int K,
   a.qy = make_qcoeff(c.ay);
   a.qx = make_qcoeff(c.ax);
   a.guard = guard_bits(c, K);
+  // the planes whose outputs set the next scale: the geometry's own planes
+  // of the internal z axis (all of them unless a slab names its own)
+  a.or_z0 = 0;
+  a.or_z1 = a.nz;
+  if (g.own_n > 0 && g.jz == 0) {
+    const int p0 = (int)g.own0, p1 = (int)(g.own0 + g.own_n);  // physical
+    a.or_z0 = a.fz ? a.nz - p1 : p0;
+    a.or_z1 = a.fz ? a.nz - p0 : p1;
+  }
   return a;
 }
 
@@ -269,6 +278,42 @@ size_t fixed_scratch_bytes() { return 3 * sizeof(ScaleSlot) + 4 * sizeof(int); }
 
 int* fixed_error_word(double* d_scratch) { return (int*)((ScaleSlot*)d_scratch + 3); }
 
+int launch_scale_prepass(const Geom& g, const double* f, double* d_scratch, cudaStream_t s) {
+  ScaleSlot* slots = (ScaleSlot*)d_scratch;
+  // max|f| over the geometry's own planes of axis 0 (all planes unless a
+  // slab names its own: its halo planes hold other ranks' values)
+  uint64_t first = 0, count = g.ntot;
+  if (g.own_n > 0) {
+    const uint64_t plane = g.ntot / g.n[0];
+    first = g.own0 * plane;
+    count = g.own_n * plane;
+  }
+  k_slots_init<<<1, 32, 0, s>>>(slots);
+  uint64_t blocks = (count + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_absmax_bits<<<(unsigned)blocks, 256, 0, s>>>(f + first, count, slots);
+  note_launch(2);
+  FDB_CUDA_TRY(cudaGetLastError());
+  return FDB_OK;
+}
+
+int launch_fixed_block(const Geom& g, const Coeffs3& c, int k, const FixedTuning& tune,
+                       int guard_K, double** buf, int* cur, bool in_f64, bool out_f64,
+                       double* d_scratch, int i, cudaStream_t s) {
+  if (fault_injected("launch")) return fail(FDB_ERR_INJECTED, "injected launch failure");
+  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : kDefaultShape;
+  FDB_TRY(launch_fixed_one(g, c, shape, k, buf[*cur], buf[*cur ^ 1], in_f64, out_f64,
+                           (ScaleSlot*)d_scratch, i, fixed_error_word(d_scratch), tune.tz, guard_K,
+                           nullptr, s));
+  *cur ^= 1;
+  return FDB_OK;
+}
+
+uint64_t* scale_word(double* d_scratch, int i) {
+  return reinterpret_cast<uint64_t*>(&((ScaleSlot*)d_scratch + (i % 3))->m);
+}
+
 int launch_advect_fixed(const Geom& g, const Coeffs3& c, int steps, int depth, double** buf,
                         int* cur, double* d_scratch, size_t scratch_bytes, cudaStream_t s) {
   FixedTuning t;
@@ -289,12 +334,7 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : kDefaultShape;
   int i0 = (scale_slot && *scale_slot >= 0) ? *scale_slot : -1;
   if (i0 < 0) {
-    k_slots_init<<<1, 32, 0, s>>>(slots);
-    uint64_t blocks = (g.ntot + 255) / 256;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    k_absmax_bits<<<(unsigned)blocks, 256, 0, s>>>(buf[*cur], g.ntot, slots);
-    note_launch(2);
-    FDB_CUDA_TRY(cudaGetLastError());
+    FDB_TRY(launch_scale_prepass(g, buf[*cur], d_scratch, s));
     i0 = 0;
   }
   const int nlaunch = (steps + K - 1) / K;

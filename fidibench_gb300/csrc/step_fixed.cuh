@@ -34,6 +34,9 @@ struct FixedArgs {
   ScaleSlot* slot_reset;
   int* err;
   int* scale_log;  // nullable: block 0 records the scale of this launch's output
+  // logical z range [or_z0, or_z1) of the planes whose outputs enter the OR
+  // of |F| (all planes, except in a slab of a distributed grid: its own ones)
+  int or_z0, or_z1;
   // STORE_G launches (the adjoint's recompute): level t+1 of every output
   // cell, in state_g units, into gout[t]; scale_log[t] receives the scale
   int32_t* gout[4];
@@ -279,11 +282,12 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
     }
     if (p >= K) {
       int64_t* dst = out + po;
+      const bool counted = lz >= a.or_z0 && lz < a.or_z1;  // uniform per plane
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (row_mask & (1u << r)) {
           const int64_t v = cur[r];
-          my_or |= (unsigned long long)(v ^ (v >> 63));
+          if (counted) my_or |= (unsigned long long)(v ^ (v >> 63));
           if (out_f64)
             dst[roff[r]] = __double_as_longlong(to_double(v, s));
           else

@@ -23,15 +23,21 @@ term, and computeCheckSum reduces the local sums with MPI_Reduce
   point-to-point: NCCL on device tensors, or gloo through host buffers);
 - the checksum is the sum of the ranks' own-plane checksums (all-reduced).
 
-Under FDB_ARITH_EXACT (and FMA) every own cell of every rank is bit-identical
-to the whole-grid run; under the block-fixed-point arithmetic each slab picks
-its own scale, which stays within the 1e-13 bar.  `SlabRing` runs all slabs
-of a decomposition in one process on one GPU with the same exchange done by
+Every slab advances in a block chain (fdb_upwind_block_begin /
+fdb_upwind_advect_block): under the block-fixed-point arithmetic the field
+stays int64 between blocks, the halo planes travel as int64, and before each
+block the ranks make their scale words equal to the maximum over all ranks
+(the scale is measured over each slab's own planes only), so every slab
+advances with the scale of the whole grid.  The result is then the
+single-field advect's bit for bit, in every arithmetic (EXACT and FMA are
+per-cell FP64 and need no agreement).  `SlabRing` runs all slabs of a
+decomposition in one process on one GPU with the same exchange done by
 device copies (tests, and single-GPU runs of the sharded form).
 
 The slab protocol (`UpwindSlab` on the GPU; any object with the same methods,
 such as a CPU stand-in in the tests): own / halo / send plane ranges,
-get_planes / set_planes / advect / checksum_own / set_own / get_own.
+get_planes / set_planes / block_begin / advect_block / get_scale_word /
+set_scale_word / checksum_own / set_own / get_own.
 """
 from __future__ import annotations
 
@@ -105,9 +111,13 @@ class UpwindSlab:
         check(lib.fdb_upwind_create_slab(self.ndims, v.ctypes.data, L.ctypes.data,
                                          n.ctypes.data, layout.planes, ctypes.byref(h)))
         self._h = h
-        check(lib.fdb_upwind_set_arith(self._h, _capi.ARITH_NAMES[arith], int(depth)))
+        # blocks of up to `halo` steps: the fixed kernel's depth is the halo
+        # depth unless one is asked for (at least the halo depth)
+        check(lib.fdb_upwind_set_arith(self._h, _capi.ARITH_NAMES[arith],
+                                       int(depth) if depth else layout.halo))
         if coeff_form != "cxx":
             check(lib.fdb_upwind_set_coeff_form(self._h, _capi.COEFF_NAMES[coeff_form]))
+        check(lib.fdb_upwind_set_own_planes(self._h, layout.own[0], layout.own[1]))
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -133,6 +143,24 @@ class UpwindSlab:
 
     def advect(self, steps: int, dt: float) -> None:
         check(lib.fdb_upwind_advect(self._h, int(steps), float(dt)))
+
+    def block_begin(self, dt: float) -> bool:
+        """Open a block chain; True when it runs the fixed-point arithmetic
+        (whose scale word the ranks must agree on before every block)."""
+        fixed = ctypes.c_int()
+        check(lib.fdb_upwind_block_begin(self._h, float(dt), ctypes.byref(fixed)))
+        return bool(fixed.value)
+
+    def advect_block(self, steps: int, dt: float, last: bool) -> None:
+        check(lib.fdb_upwind_advect_block(self._h, int(steps), float(dt), 1 if last else 0))
+
+    def get_scale_word(self, out) -> None:
+        is_dev = 1 if getattr(out, "is_cuda", False) else 0
+        check(lib.fdb_upwind_get_scale_word(self._h, _capi.dptr(out), is_dev))
+
+    def set_scale_word(self, src) -> None:
+        is_dev = 1 if getattr(src, "is_cuda", False) else 0
+        check(lib.fdb_upwind_set_scale_word(self._h, _capi.dptr(src), is_dev))
 
     def checksum_own(self) -> float:
         out = ctypes.c_double()
@@ -170,14 +198,23 @@ class UpwindSlab:
         return {v: k for k, v in _capi.ARITH_NAMES.items()}.get(a.value, str(a.value))
 
 
-def _advance(slabs_and_exchange, steps: int, dt: float, halo: int) -> None:
-    exchange, slabs = slabs_and_exchange
+def _advance(slabs, exchange, agree, steps: int, dt: float, halo: int) -> None:
+    """steps steps in blocks of up to `halo`: the halo exchange before every
+    block and, under the fixed-point arithmetic, the scale agreement."""
+    if steps == 0:
+        return
+    fixed = [s.block_begin(dt) for s in slabs]
+    if any(fixed) != all(fixed):
+        raise RuntimeError("slabs disagree on the arithmetic")
+    fixed = fixed[0]
     done = 0
     while done < steps:
         k = min(halo, steps - done)
         exchange()
+        if fixed:
+            agree()
         for s in slabs:
-            s.advect(k, dt)
+            s.advect_block(k, dt, done + k == steps)
         done += k
 
 
@@ -224,14 +261,17 @@ class DistributedUpwind:
             slab = slab_factory(self.layout)
         self.slab = slab
         n = self.halo * self.plane
+        # halo planes hold FP64 or int64 values: 8-byte words moved as they are
         if self.on_device:
             dev = torch.device("cuda", torch.cuda.current_device())
             self._send = torch.empty(n, dtype=torch.float64, device=dev)
             self._recv = torch.empty(n, dtype=torch.float64, device=dev)
+            self._word = torch.zeros(1, dtype=torch.int64, device=dev)
         else:
             pin = torch.cuda.is_available() and isinstance(self.slab, UpwindSlab)
             self._send = torch.empty(n, dtype=torch.float64, pin_memory=pin)
             self._recv = torch.empty(n, dtype=torch.float64, pin_memory=pin)
+            self._word = torch.zeros(1, dtype=torch.int64, pin_memory=pin)
 
     def close(self) -> None:
         if hasattr(self.slab, "close"):
@@ -290,12 +330,29 @@ class DistributedUpwind:
                 req.wait()
         self.slab.set_planes(lay.halo_at[0], lay.halo_at[1], self._recv)
 
+    def agree_scale(self) -> None:
+        """Every rank's scale word <- the maximum over the ranks (the scale
+        words are FP64 bit patterns of max|f| or ORs of |F|: non-negative,
+        ordered as integers)."""
+        import torch
+        import torch.distributed as dist
+        if self.world == 1:
+            return
+        self.slab.get_scale_word(self._word)
+        if self.on_device:
+            with torch.cuda.stream(self.stream):
+                dist.all_reduce(self._word, op=dist.ReduceOp.MAX, group=self.group)
+        else:
+            dist.all_reduce(self._word, op=dist.ReduceOp.MAX, group=self.group)
+        self.slab.set_scale_word(self._word)
+
     def advect(self, numTimeSteps: int, deltaTime: float) -> None:
-        """numTimeSteps steps of the global problem: exchange, then up to K
-        steps on every slab, repeated."""
+        """numTimeSteps steps of the global problem: exchange (and agree on
+        the scale), then up to K steps on every slab, repeated."""
         if numTimeSteps < 0:
             raise ValueError("numTimeSteps must be >= 0")
-        _advance((self.exchange, [self.slab]), int(numTimeSteps), float(deltaTime), self.halo)
+        _advance([self.slab], self.exchange, self.agree_scale, int(numTimeSteps),
+                 float(deltaTime), self.halo)
 
     def checksum(self) -> float:
         """Sum of the global field (Filter::computeCheckSum, Filter.cpp:465-485;
@@ -341,6 +398,7 @@ class SlabRing:
         dev = torch.device("cuda", torch.cuda.current_device())
         self._tmp = [torch.empty(self.halo * self.plane, dtype=torch.float64, device=dev)
                      for _ in range(world)]
+        self._words = torch.zeros(world, dtype=torch.int64, device=dev)
 
     def close(self) -> None:
         for s in self.slabs:
@@ -363,10 +421,22 @@ class SlabRing:
             lay = self.layouts[r]
             s.set_planes(lay.halo_at[0], lay.halo_at[1], self._tmp[lay.upwind])
 
+    def agree_scale(self) -> None:
+        # every slab's scale word -> one tensor, its maximum back to every slab
+        import torch
+        for r, s in enumerate(self.slabs):
+            s.get_scale_word(self._words[r:r + 1])
+        with torch.cuda.stream(self.stream):
+            m = torch.max(self._words).reshape(1)
+            for s in self.slabs:
+                s.set_scale_word(m)
+            self._m = m  # kept alive until the copies out of it have run
+
     def advect(self, numTimeSteps: int, deltaTime: float) -> None:
         if numTimeSteps < 0:
             raise ValueError("numTimeSteps must be >= 0")
-        _advance((self.exchange, self.slabs), int(numTimeSteps), float(deltaTime), self.halo)
+        _advance(self.slabs, self.exchange, self.agree_scale, int(numTimeSteps),
+                 float(deltaTime), self.halo)
 
     def checksum(self) -> float:
         return float(sum(s.checksum_own() for s in self.slabs))

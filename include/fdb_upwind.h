@@ -141,6 +141,36 @@ int fdb_upwind_get_planes(fdb_upwind* h, uint64_t first, uint64_t count, double*
 int fdb_upwind_set_planes(fdb_upwind* h, uint64_t first, uint64_t count, const double* src,
                           int is_device);
 
+/* The planes [first, first + count) of axis 0 that this handle owns (a slab's
+ * planes without its halo; default: all).  The fixed-point arithmetic measures
+ * its scale over them only, so that the slabs of a distributed grid can agree
+ * on the scale of the whole grid (fdb_upwind_get/set_scale_word).  The
+ * restriction applies when axis 0 is the handle's third-from-last axis (3-D
+ * grids); other grids measure every plane. */
+int fdb_upwind_set_own_planes(fdb_upwind* h, uint64_t first, uint64_t count);
+
+/* Block-wise advance for a caller that exchanges halo planes between blocks
+ * of steps (the distributed form: upwindMpi.cxx advances one step between
+ * two halo fetches, Filter.cpp:212-221; here a block is up to the halo depth
+ * of steps).  fdb_upwind_block_begin(h, dt, &fixed) opens a chain with the
+ * arithmetic advect(dt) would use (fixed = 1 for the block-fixed-point one);
+ * each fdb_upwind_advect_block(h, steps, dt, last) then advances `steps`
+ * steps, `last` = 1 closing the chain.  Under the fixed-point arithmetic the
+ * field stays int64 between blocks (FP64 before the first and after the
+ * last), each block is one launch of at most the handle's temporal depth of
+ * steps, and a chain of blocks of that depth (the last one shorter) gives
+ * the field advect(total steps) gives, bit for bit.  Between blocks a caller
+ * may move planes with fdb_upwind_get/set_planes (raw 8-byte copies) and must
+ * make every slab's scale word equal to the maximum over the slabs
+ * (fdb_upwind_get/set_scale_word, device pointers, stream-ordered): then the
+ * slabs of a grid advance with one scale, exactly as the whole grid would.
+ * While a chain is open the calls that read or write the field as FP64
+ * return FDB_ERR_INVALID.  No reference counterpart. */
+int fdb_upwind_block_begin(fdb_upwind* h, double dt, int* fixed);
+int fdb_upwind_advect_block(fdb_upwind* h, int steps, double dt, int last);
+int fdb_upwind_get_scale_word(fdb_upwind* h, uint64_t* dst, int is_device);
+int fdb_upwind_set_scale_word(fdb_upwind* h, const uint64_t* src, int is_device);
+
 /* checksum() of planes [first, first + count) of axis 0 only (a slab's own
  * planes, without its halo): the local sum of Filter::computeCheckSum
  * (Filter.cpp:465-482); the caller reduces over ranks.  Synchronises. */

@@ -49,6 +49,12 @@ class OracleSlab:
         self.f = self.port.advect_spacing(self.n_ext, self.v, self.L, self.n_global, self.f, k,
                                           dt, coeff_form=self.form)
 
+    def block_begin(self, dt):
+        return False  # FP64 steps: no scale to agree on
+
+    def advect_block(self, k, dt, last):
+        self.advect(k, dt)
+
     def checksum_own(self):
         return self.port.checksum(self.f[self._rng(*self.layout.own)])
 
