@@ -882,7 +882,8 @@ int fdb_upwind_set_tuning(fdb_upwind* h, int key, int value) {
     return FDB_OK;
   }
   if (key == FDB_TUNE_SHAPE) {
-    if (value < -1 || value > 4) return fail(FDB_ERR_INVALID, "shape must be in [-1, 4]");
+    if (value < -1 || value >= fx_num_shapes())
+      return fail(FDB_ERR_INVALID, "shape must be in [-1, 6]");
     h->tune.shape = value;
     return FDB_OK;
   }

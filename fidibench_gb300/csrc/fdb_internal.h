@@ -132,6 +132,8 @@ int launch_step_generic(const Geom& g, double dt, const double* in, double* out,
 // are outside what it serves (the caller then uses the FP64 kernel).
 int fixed_supported(const Geom& g, const Coeffs3& c, int depth);
 bool fixed_preferred(const Geom& g);
+// number of CTA shapes the fixed kernel is compiled for (FDB_TUNE_SHAPE range)
+int fx_num_shapes();
 // steps per launch the fixed kernel picks for g when none is asked for
 int default_depth(const Geom& g);
 size_t fixed_scratch_bytes();
@@ -140,7 +142,8 @@ int* fixed_error_word(double* d_scratch);
 // Launch-shape knobs of the fixed kernel (0 / -1 = automatic).
 struct FixedTuning {
   int depth = 0;   // temporal depth K (steps per launch), 1..4
-  int shape = -1;  // 0 = 8x8, 1 = 4x16 (history in registers), 2 = 8x8, 3 = 4x16 (in smem)
+  int shape = -1;  // 0 = 8x8, 1 = 4x16 (history in registers), 2 = 8x8, 3 = 4x16, 4 = 4x8
+                   // (in smem), 5 = 4x8, 6 = 6x8 (in smem, register loads, x-1 from smem)
   int tz = 0;      // output planes per CTA along z
 };
 

@@ -216,6 +216,8 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
     case fx::kR8W8S: fx::launch_r8w8s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
     case fx::kR4W16S: fx::launch_r4w16s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
     case fx::kR4W8S: fx::launch_r4w8s(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    case fx::kR4W8L: fx::launch_r4w8l(K, in_f64, out_f64, cap, pin, pout, a, st); break;
+    case fx::kR6W8L: fx::launch_r6w8l(K, in_f64, out_f64, cap, pin, pout, a, st); break;
     default: fx::launch_r8w8(K, in_f64, out_f64, cap, pin, pout, a, st); break;
   }
   note_launch();
@@ -225,9 +227,11 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
 
 namespace {
 
-// Default shape: 4 rows x 8 warps with the plane history in shared memory (32
-// x 32 computed cells per tile; the fastest measured shape at 160^3 - 512^3).
-constexpr int kDefaultShape = fx::kR4W8S;
+// Default shape: 6 rows x 8 warps with the plane history in shared memory,
+// the next plane loaded into registers and the x-1 neighbour read from the
+// history (32 x 48 computed cells per tile; at 512^3 457 GCUPS against 442
+// for 4 x 8 with cp.async staging and shuffles, at 320^3 416 against 391).
+constexpr int kDefaultShape = fx::kR6W8L;
 
 }  // namespace
 
@@ -273,6 +277,8 @@ bool fixed_preferred(const Geom& g) {
   // tiles are (32-K) x (R*W-K) cells in (x, y); small grids are cheaper in FP64
   return g.ndims <= 3 && g.nx >= 16 && g.ny >= 16 && g.nz >= 8 && g.ntot >= (1u << 18);
 }
+
+int fx_num_shapes() { return fx::kNumShapes; }
 
 size_t fixed_scratch_bytes() { return 3 * sizeof(ScaleSlot) + 4 * sizeof(int); }
 

@@ -81,9 +81,9 @@ __device__ __forceinline__ int64_t update(int64_t c, int64_t zb, int64_t up, int
 
 // Dynamic shared memory of one CTA: plane prefetch [2][R][threads] (cp.async
 // loader only), plus the K-deep plane history [K][R][threads] when HSM.
-template <int K, int R, int W, bool HSM>
+template <int K, int R, int W, bool HSM, int LOADER = 0>
 constexpr int fixed_smem_bytes() {
-  return (2 + (HSM ? K : 0)) * R * 32 * W * (int)sizeof(int64_t);
+  return ((LOADER == 0 ? 2 : 0) + (HSM ? K : 0)) * R * 32 * W * (int)sizeof(int64_t);
 }
 
 // Scale of a launch (or, in the batched kernel, of one instance's time block)
@@ -119,14 +119,23 @@ __device__ __forceinline__ bool scale_from_slot(const ScaleSlot* slot, int guard
 // no other CTA writes the input during the launch), or L1-bypassing register
 // loads (the persistent batched kernel reads data that other CTAs wrote
 // earlier in the same launch, which L1 may hold stale).
-enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1 };
+// kLoadRegs: read-only-path register loads one plane ahead (one tile per
+// launch, like cp.async, but without the shared-memory staging).
+enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1, kLoadRegs = 2 };
 
 // Advance one tile of one field by `levels` (<= K) steps.  The tile's output
 // region is x in [X0, X0+tx), y in [Y0, Y0+ty), z in [Z0, Z0+nout) of the
 // logical axes (Z0 + nout <= nz); the CTA computes a (32) x (R*W) x (nout+K)
 // region that starts K cells upstream on every axis.  my_or accumulates |F| bits of the stored
 // outputs.  Callers synchronise the CTA before reusing shared memory.
-template <int K, int R, int W, bool HSM, int LOADER, bool STORE_G = false>
+//
+// LEFT_SMEM (with HSM): the x-1 neighbour comes from the plane history
+// instead of a shuffle: each level's values go into their history slot
+// before the update (the previous plane's were read just before), and lane l
+// reads lane l-1's slot after a warp barrier.  Same values, fewer FMA-pipe
+// moves than the 64-bit shuffle.
+template <int K, int R, int W, bool HSM, int LOADER, bool STORE_G = false,
+          bool LEFT_SMEM = false>
 __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int Z0,
                                              int nout, int levels, bool in_f64, bool out_f64, int s, int d,
                                              const int64_t* __restrict__ in,
@@ -175,7 +184,8 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
 
   int64_t hist[HSM ? 1 : K][R];
   int64_t cur[R];
-  int64_t pre[LOADER == kLoadL2Regs ? R : 1];
+  static_assert(!LEFT_SMEM || HSM, "the x-1 neighbour from shared memory needs the history there");
+  int64_t pre[LOADER != kLoadCpAsync ? R : 1];
 #pragma unroll
   for (int t = 0; t < (HSM ? 1 : K); ++t)
 #pragma unroll
@@ -198,7 +208,8 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
       cp_async_commit();
     } else {
 #pragma unroll
-      for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + roff[r]);
+      for (int r = 0; r < R; ++r)
+        pre[r] = LOADER == kLoadRegs ? __ldg(src + roff[r]) : __ldcg(src + roff[r]);
     }
   }
 
@@ -223,7 +234,8 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
       if (p + 1 < nplanes) {
         const int64_t* src = in + po_next;
 #pragma unroll
-        for (int r = 0; r < R; ++r) pre[r] = __ldcg(src + roff[r]);
+        for (int r = 0; r < R; ++r)
+          pre[r] = LOADER == kLoadRegs ? __ldg(src + roff[r]) : __ldcg(src + roff[r]);
       }
     }
     if (in_f64) {
@@ -257,15 +269,25 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
       s_row[parity][warp][lane] = cur[R - 1];
       // x-1 neighbour; lane 0 (the tile's halo column) receives its own value
       int64_t left[R];
+      if (LEFT_SMEM) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
+        for (int r = 0; r < R; ++r) s_hist[t][r][tid] = cur[r];
+        __syncwarp();
+        const int src_tid = tid - (lane > 0 ? 1 : 0);
+#pragma unroll
+        for (int r = 0; r < R; ++r) left[r] = s_hist[t][r][src_tid];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) left[r] = __shfl_up_sync(0xffffffffu, cur[r], 1);
+      }
       auto row = [&](int r, int64_t upv) {
         const int64_t c = cur[r];
         const int64_t nv = update(c, HSM ? zb[r] : hist[HSM ? 0 : t][r], upv, left[r], a);
-        if (HSM)
-          s_hist[t][r][tid] = c;
-        else
+        if (HSM) {
+          if (!LEFT_SMEM) s_hist[t][r][tid] = c;
+        } else {
           hist[HSM ? 0 : t][r] = c;
+        }
         cur[r] = nv;
       };
 #pragma unroll
@@ -325,7 +347,8 @@ __device__ __forceinline__ void cta_or(unsigned long long my_or, unsigned long l
 // their halo rows through L2, and the slabs shrink towards the end of the
 // grid so that the last wave is short (the scheduler hands out CTAs in
 // index order).
-template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64, bool STORE_G = false>
+template <int K, int R, int W, bool HSM, int MINB, bool IN_F64, bool OUT_F64, bool STORE_G = false,
+          int LOAD = kLoadCpAsync, bool LEFT = false>
 __global__ void __launch_bounds__(32 * W, MINB)
 k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const FixedArgs a) {
   extern __shared__ __align__(16) int64_t s_dyn[];
@@ -354,19 +377,24 @@ k_advect_fixed(const int64_t* __restrict__ in, int64_t* __restrict__ out, const 
     }
   }
   unsigned long long my_or = 0ull;
-  advance_tile<K, R, W, HSM, kLoadCpAsync, STORE_G>(a, tile % a.tiles_x, tile / a.tiles_x, z0,
-                                                    nout, K, IN_F64, OUT_F64, s, d, in, out,
-                                                    s_dyn, s_row, my_or);
+  advance_tile<K, R, W, HSM, LOAD, STORE_G, LEFT>(a, tile % a.tiles_x, tile / a.tiles_x, z0,
+                                                  nout, K, IN_F64, OUT_F64, s, d, in, out,
+                                                  s_dyn, s_row, my_or);
   cta_or<W>(my_or, s_or, &a.slot_out->m);
 }
 
 // Kernel shapes compiled into the library: rows per thread x warps per CTA,
-// history in registers (reg) or shared memory (smem).
-enum Shape { kR8W8 = 0, kR4W16 = 1, kR8W8S = 2, kR4W16S = 3, kR4W8S = 4, kNumShapes = 5 };
-constexpr int shape_rows(int sh) { return (sh == kR8W8 || sh == kR8W8S) ? 8 : 4; }
-constexpr int shape_warps(int sh) {
-  return (sh == kR8W8 || sh == kR8W8S || sh == kR4W8S) ? 8 : 16;
+// history in registers (reg) or shared memory (smem); the L shapes load the
+// next plane into registers and take the x-1 neighbour from the history
+// (kLoadRegs, LEFT_SMEM).
+enum Shape {
+  kR8W8 = 0, kR4W16 = 1, kR8W8S = 2, kR4W16S = 3, kR4W8S = 4, kR4W8L = 5, kR6W8L = 6,
+  kNumShapes = 7
+};
+constexpr int shape_rows(int sh) {
+  return (sh == kR8W8 || sh == kR8W8S) ? 8 : (sh == kR6W8L ? 6 : 4);
 }
+constexpr int shape_warps(int sh) { return (sh == kR4W16 || sh == kR4W16S) ? 16 : 8; }
 
 // z-slabs of one k_advect_fixed launch for `resident` CTAs on the GPU at once:
 // slabs of h0 planes (cap if > 0, else about a quarter of the planes per
@@ -374,17 +402,16 @@ constexpr int shape_warps(int sh) {
 // resident CTA down to 8.  Sets a.nslab / a.slab_z; returns the CTA count.
 long long plan_slabs(FixedArgs& a, int resident, int cap);
 
-template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT, bool STORE_G = false>
+template <int K, int R, int W, bool HSM, int MINB, bool IN, bool OUT, bool STORE_G = false,
+          int LOAD = kLoadCpAsync, bool LEFT = false>
 void launch_k(int cap, const int64_t* in, int64_t* out, FixedArgs a, cudaStream_t st) {
-  constexpr int smem = fixed_smem_bytes<K, R, W, HSM>();
+  constexpr int smem = fixed_smem_bytes<K, R, W, HSM, LOAD>();
+  auto kern = k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G, LOAD, LEFT>;
   static int per_sm = -1;  // per instantiation; benign race (idempotent)
   if (per_sm < 0) {
-    cudaFuncSetAttribute(k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>, 32 * W, smem) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * W, smem) != cudaSuccess)
       occ = 1;
     per_sm = occ > 0 ? occ : 1;
   }
@@ -393,8 +420,7 @@ void launch_k(int cap, const int64_t* in, int64_t* out, FixedArgs a, cudaStream_
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long blocks = plan_slabs(a, per_sm * (sms > 0 ? sms : 1), cap);
   if (blocks <= 0) return;
-  k_advect_fixed<K, R, W, HSM, MINB, IN, OUT, STORE_G>
-      <<<(unsigned)blocks, 32 * W, smem, st>>>(in, out, a);
+  kern<<<(unsigned)blocks, 32 * W, smem, st>>>(in, out, a);
 }
 
 // int64 in and out, every level also stored in state_g units (a.gout)
@@ -409,23 +435,27 @@ void launch_shape_store_g(int K, int cap, const int64_t* in, int64_t* out, const
   }
 }
 
-template <int K, int R, int W, bool HSM, int MINB>
+template <int K, int R, int W, bool HSM, int MINB, int LOAD = kLoadCpAsync, bool LEFT = false>
 void launch_io(bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,
                const FixedArgs& a, cudaStream_t st) {
-  if (in_f64 && out_f64) launch_k<K, R, W, HSM, MINB, true, true>(cap, in, out, a, st);
-  else if (in_f64) launch_k<K, R, W, HSM, MINB, true, false>(cap, in, out, a, st);
-  else if (out_f64) launch_k<K, R, W, HSM, MINB, false, true>(cap, in, out, a, st);
-  else launch_k<K, R, W, HSM, MINB, false, false>(cap, in, out, a, st);
+  if (in_f64 && out_f64)
+    launch_k<K, R, W, HSM, MINB, true, true, false, LOAD, LEFT>(cap, in, out, a, st);
+  else if (in_f64)
+    launch_k<K, R, W, HSM, MINB, true, false, false, LOAD, LEFT>(cap, in, out, a, st);
+  else if (out_f64)
+    launch_k<K, R, W, HSM, MINB, false, true, false, LOAD, LEFT>(cap, in, out, a, st);
+  else
+    launch_k<K, R, W, HSM, MINB, false, false, false, LOAD, LEFT>(cap, in, out, a, st);
 }
 
-template <int R, int W, bool HSM, int MINB>
+template <int R, int W, bool HSM, int MINB, int LOAD = kLoadCpAsync, bool LEFT = false>
 void launch_shape(int K, bool in_f64, bool out_f64, int cap, const int64_t* in, int64_t* out,
                   const FixedArgs& a, cudaStream_t st) {
   switch (K) {
-    case 1: launch_io<1, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
-    case 2: launch_io<2, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
-    case 3: launch_io<3, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
-    default: launch_io<4, R, W, HSM, MINB>(in_f64, out_f64, cap, in, out, a, st); break;
+    case 1: launch_io<1, R, W, HSM, MINB, LOAD, LEFT>(in_f64, out_f64, cap, in, out, a, st); break;
+    case 2: launch_io<2, R, W, HSM, MINB, LOAD, LEFT>(in_f64, out_f64, cap, in, out, a, st); break;
+    case 3: launch_io<3, R, W, HSM, MINB, LOAD, LEFT>(in_f64, out_f64, cap, in, out, a, st); break;
+    default: launch_io<4, R, W, HSM, MINB, LOAD, LEFT>(in_f64, out_f64, cap, in, out, a, st); break;
   }
 }
 
@@ -456,6 +486,8 @@ FDB_FX_DECLARE(launch_r4w16)
 FDB_FX_DECLARE(launch_r8w8s)
 FDB_FX_DECLARE(launch_r4w16s)
 FDB_FX_DECLARE(launch_r4w8s)
+FDB_FX_DECLARE(launch_r4w8l)
+FDB_FX_DECLARE(launch_r6w8l)
 #undef FDB_FX_DECLARE
 
 }  // namespace fx

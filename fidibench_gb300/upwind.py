@@ -103,7 +103,9 @@ class Upwind:
     def set_shape(self, shape: int) -> None:
         """Fixed-point kernel CTA shape: 0 = 8 rows x 8 warps, 1 = 4 x 16 (plane
         history in registers), 2 = 8 x 8, 3 = 4 x 16, 4 = 4 x 8 (history in
-        shared memory), -1 = automatic (3)."""
+        shared memory), 5 = 4 x 8, 6 = 6 x 8 (history in shared memory, the
+        next plane in registers, the x-1 neighbour from the history),
+        -1 = automatic."""
         check(lib.fdb_upwind_set_tuning(self._h, 2, int(shape)))
 
     def set_adjoint_form(self, form: str = "closed") -> None:

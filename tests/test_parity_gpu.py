@@ -165,7 +165,7 @@ def test_step_counts_fixed_blocking(fdb, port, steps):
     assert cs == pytest.approx(port.checksum(ref), rel=SUM_TOL)
 
 
-@pytest.mark.parametrize("shape", [3, 4, 0])
+@pytest.mark.parametrize("shape", [3, 4, 0, 5, 6])
 @pytest.mark.parametrize("tile_z", [0, 1, 3, 17])
 @pytest.mark.parametrize("n", [(37, 70, 45), (64, 64, 64), (9, 130, 33)])
 def test_z_run_split_vs_oracle(fdb, port, n, tile_z, shape):
@@ -202,14 +202,14 @@ def test_shapes_bit_identical(fdb, port, n, v, depth):
     f0 = rng.standard_normal(int(np.prod(n)))
     dt = 0.3 * min(Lj / nj for Lj, nj in zip(L, n))
     outs = {}
-    for shape in range(5):
+    for shape in range(7):
         up = fdb.Upwind(v, L, n, arith="fixed", depth=depth)
         up.set_shape(shape)
         up.f = f0
         up.advect(11, dt)
         outs[shape] = up.f
         up.close()
-    for shape in range(5):
+    for shape in range(7):
         assert np.array_equal(outs[shape], outs[4]), shape
     assert rel_maxnorm(outs[4], port.advect(n, v, L, f0, 11, dt)) <= FIELD_TOL
 
