@@ -134,7 +134,7 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
     int64_t* out = ((b & 1) ? arena0 : arena1) + I.offset;
     unsigned long long my_or = 0ull;
     const int z0 = tz * I.a.tz;
-    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs, false, true>(I.a, tx, ty, z0, min(I.a.tz, I.a.nz - z0),
+    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(I.a, tx, ty, z0, min(I.a.tz, I.a.nz - z0),
                                                      levels, b == 0, b == nblocks - 1, s, d, in,
                                                      out, s_dyn, s_row, my_or);
     fx::cta_or<W>(my_or, s_or, &sl[(b + 1) % 3].m);
@@ -325,9 +325,6 @@ const Variant kVariants[] = {
     {2, fx::kR8W8S, launch_batch_kernel<2, 8, 8>, resident_ctas_of<2, 8, 8>},
     {3, fx::kR8W8S, launch_batch_kernel<3, 8, 8>, resident_ctas_of<3, 8, 8>},
     {4, fx::kR8W8S, launch_batch_kernel<4, 8, 8>, resident_ctas_of<4, 8, 8>},
-    {2, fx::kR6W8L, launch_batch_kernel<2, 6, 8>, resident_ctas_of<2, 6, 8>},
-    {3, fx::kR6W8L, launch_batch_kernel<3, 6, 8>, resident_ctas_of<3, 6, 8>},
-    {4, fx::kR6W8L, launch_batch_kernel<4, 6, 8>, resident_ctas_of<4, 6, 8>},
 };
 
 const Variant* find_variant(int K, int shape) {
@@ -872,9 +869,8 @@ int fdb_batch_set_tuning(fdb_batch* b, int key, int value) {
     if (value < 0 || value == 1 || value > 4) return fail(FDB_ERR_INVALID, "batched depth is 0, 2, 3 or 4");
     b->K = value;
   } else if (key == FDB_TUNE_SHAPE) {
-    if (!(value == -1 || value == fx::kR4W16S || value == fx::kR4W8S || value == fx::kR8W8S ||
-          value == fx::kR6W8L))
-      return fail(FDB_ERR_INVALID, "batched shape is -1, 2 (8x8), 3 (4x16), 4 (4x8) or 6 (6x8)");
+    if (!(value == -1 || value == fx::kR4W16S || value == fx::kR4W8S || value == fx::kR8W8S))
+      return fail(FDB_ERR_INVALID, "batched shape is -1, 2 (8x8), 3 (4x16) or 4 (4x8)");
     b->shape = value;
   } else if (key == FDB_TUNE_TILE_Z) {
     if (value < 0) return fail(FDB_ERR_INVALID, "tile_z must be >= 0");

@@ -227,11 +227,16 @@ int launch_fixed_one(const Geom& g, const Coeffs3& c, int shape, int K, const vo
 
 namespace {
 
-// Default shape: 6 rows x 8 warps with the plane history in shared memory,
-// the next plane loaded into registers and the x-1 neighbour read from the
-// history (32 x 48 computed cells per tile; at 512^3 457 GCUPS against 442
-// for 4 x 8 with cp.async staging and shuffles, at 320^3 416 against 391).
-constexpr int kDefaultShape = fx::kR6W8L;
+// Default shape: 4 or 6 rows x 8 warps with the plane history in shared
+// memory, the next plane loaded into registers and the x-1 neighbour read
+// from the history.  Measured (advect(100), one GB300): 512^3 457 GCUPS for
+// 6 rows against 454 for 4 rows and 442 for the cp.async/shuffle 4 x 8 form;
+// 384^3 422 / 418 / 418; 320^3 416 / 395 / 391; 256^3 389 / 394 / 382.
+// Grids of up to 256^3 cells take 4 rows (more tiles keep the GPU full).
+int default_shape(const Geom& g, int K) {
+  (void)K;
+  return g.ntot > (uint64_t)256 * 256 * 256 ? fx::kR6W8L : fx::kR4W8L;
+}
 
 }  // namespace
 
@@ -308,7 +313,8 @@ int launch_fixed_block(const Geom& g, const Coeffs3& c, int k, const FixedTuning
                        int guard_K, double** buf, int* cur, bool in_f64, bool out_f64,
                        double* d_scratch, int i, cudaStream_t s) {
   if (fault_injected("launch")) return fail(FDB_ERR_INJECTED, "injected launch failure");
-  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : kDefaultShape;
+  const int shape =
+      (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : default_shape(g, guard_K);
   FDB_TRY(launch_fixed_one(g, c, shape, k, buf[*cur], buf[*cur ^ 1], in_f64, out_f64,
                            (ScaleSlot*)d_scratch, i, fixed_error_word(d_scratch), tune.tz, guard_K,
                            nullptr, s));
@@ -337,7 +343,8 @@ int launch_advect_fixed_ex(const Geom& g, const Coeffs3& c, int steps, const Fix
   ScaleSlot* slots = (ScaleSlot*)d_scratch;
   int* err = fixed_error_word(d_scratch);
   const int K = tune.depth > 0 ? tune.depth : default_depth(g);
-  const int shape = (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : kDefaultShape;
+  const int shape =
+      (tune.shape >= 0 && tune.shape < fx::kNumShapes) ? tune.shape : default_shape(g, K);
   int i0 = (scale_slot && *scale_slot >= 0) ? *scale_slot : -1;
   if (i0 < 0) {
     FDB_TRY(launch_scale_prepass(g, buf[*cur], d_scratch, s));
