@@ -820,7 +820,12 @@ def main() -> None:
 
     sharded = None
     if not args.no_sharded:
-        sharded = bench_sharded(max(1, min(args.steps, 3)), 1, ws)
+        # the headline line must survive a failure of this secondary leg (its
+        # multi-rank transfers have not run on more than one GPU here)
+        try:
+            sharded = bench_sharded(max(1, min(args.steps, 3)), 1, ws)
+        except Exception as exc:  # noqa: BLE001
+            sharded = {"error": f"{type(exc).__name__}: {str(exc)[:300]}"}
 
     batched = None
     if not args.no_batch:
