@@ -24,9 +24,14 @@ field = sphere indicator (centre 0.5^3, radius 0.2) + seeded uniform noise in
                this tree, else the oracle's C restatement) on the host cores,
                on a bounded sample of the same workload.
 
+  f64_paths    the FP64 arithmetics (EXACT, FMA) at the same workload.
+  sharded      the distributed form: one (512 N) x 512 x 512 grid split into
+               512-plane slabs, one per rank, halo planes exchanged every 3
+               steps (NCCL between ranks, a device copy at N = 1).
+
 `--impl reference` times that CPU implementation alone (the reference arm).
-Under torchrun (N > 1) every rank runs an independent replica ("replicas
-only": the plain form does not shard) and rank 0 prints the aggregate.
+Under torchrun (N > 1) the headline runs one independent replica per rank and
+rank 0 prints the aggregate; the sharded leg splits one grid over the ranks.
 """
 from __future__ import annotations
 
