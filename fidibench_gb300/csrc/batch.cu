@@ -83,6 +83,7 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
   __shared__ unsigned long long s_or[W];
   __shared__ int s_w;
   __shared__ int s_stop;
+  __shared__ __align__(16) FixedArgs s_a;
 
   const long long total = (long long)nblocks * items_per_block;
   for (;;) {
@@ -98,6 +99,16 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
     const int i = item_inst[item];
     const InstDev& I = insts[i];
     const int local = item - I.item_base;
+    // the item's FixedArgs into shared memory: under the register cap the
+    // tile loop re-reads the coefficients at every level, and a shared-memory
+    // read is cheaper than a global one (the previous item's readers passed
+    // the barrier at the end of its iteration)
+    {
+      static_assert(sizeof(FixedArgs) % 4 == 0, "FixedArgs is copied as 32-bit words");
+      const int* src = reinterpret_cast<const int*>(&I.a);
+      int* dst = reinterpret_cast<int*>(&s_a);
+      for (int k = threadIdx.x; k < (int)(sizeof(FixedArgs) / 4); k += blockDim.x) dst[k] = src[k];
+    }
 
     // wait until every block b-1 tile of this instance is done
     if (threadIdx.x == 0 && b > 0) {
@@ -117,7 +128,7 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
 
     ScaleSlot* sl = slots + 3 * i;
     int s, d;
-    if (!scale_from_slot(sl + (b % 3), I.a.guard, &s, &d) && threadIdx.x == 0) atomicOr(err, 1);
+    if (!scale_from_slot(sl + (b % 3), s_a.guard, &s, &d) && threadIdx.x == 0) atomicOr(err, 1);
     if (local == 0 && threadIdx.x == 0) {
       ScaleSlot* rs = sl + ((b + 2) % 3);
       rs->m = 0ull;
@@ -125,16 +136,16 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
       sl[(b + 1) % 3].s = s;
       sl[(b + 1) % 3].kind = 1;
     }
-    const int tx = local % I.a.tiles_x;
-    const int rest = local / I.a.tiles_x;
-    const int ty = rest % I.a.tiles_y;
-    const int tz = rest / I.a.tiles_y;
+    const int tx = local % s_a.tiles_x;
+    const int rest = local / s_a.tiles_x;
+    const int ty = rest % s_a.tiles_y;
+    const int tz = rest / s_a.tiles_y;
     const int levels = min(K, steps - b * K);
     const int64_t* in = ((b & 1) ? arena1 : arena0) + I.offset;
     int64_t* out = ((b & 1) ? arena0 : arena1) + I.offset;
     unsigned long long my_or = 0ull;
-    const int z0 = tz * I.a.tz;
-    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(I.a, tx, ty, z0, min(I.a.tz, I.a.nz - z0),
+    const int z0 = tz * s_a.tz;
+    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(s_a, tx, ty, z0, min(s_a.tz, s_a.nz - z0),
                                                      levels, b == 0, b == nblocks - 1, s, d, in,
                                                      out, s_dyn, s_row, my_or);
     fx::cta_or<W>(my_or, s_or, &sl[(b + 1) % 3].m);
