@@ -62,7 +62,22 @@ struct InstDev {
   int item_base;      // first item of the instance within a block
 };
 
+// One packed tile: rectangles of gw lanes x gh warps of one instance, laid
+// out (32 / gw) across the lanes and (W / gh) down the warps, row-major from
+// groups[group_base]; each marches nout + K planes.
+struct ItemDev {
+  int inst;
+  int gw, gh;
+  int group_base;
+  int nout;
+};
+
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+// depth of the persistent launch when none is set (the kernel is issue-bound,
+// so the smaller halo of depth 2 outweighs its extra field traffic), and the
+// depth the storage order is chosen for
+constexpr int kDefaultDepth = 2;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -74,8 +89,8 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 // spills); 8-row shapes: 16 warps (their rows need the registers)
 template <int K, int R, int W>
 __global__ void __launch_bounds__(32 * W, (R > 4 ? 512 : 1024) / (32 * W))
-k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_inst,
-              int items_per_block, int nblocks, int steps, int64_t* arena0, int64_t* arena1,
+k_batch_fixed(const InstDev* __restrict__ insts, const ItemDev* __restrict__ items,
+              const fx::TileGroup* __restrict__ groups, int items_per_block, int nblocks, int steps, int64_t* arena0, int64_t* arena1,
               ScaleSlot* slots, unsigned* done, unsigned* queue, int* err, unsigned wait_bias,
               long long wait_cycles) {
   extern __shared__ __align__(16) int64_t s_dyn[];  // plane history [K][R][threads]
@@ -96,7 +111,8 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
     if (w >= total || s_stop) break;
     const int b = w / items_per_block;
     const int item = w - b * items_per_block;
-    const int i = item_inst[item];
+    const ItemDev it = items[item];
+    const int i = it.inst;
     const InstDev& I = insts[i];
     const int local = item - I.item_base;
     // the item's FixedArgs into shared memory: under the register cap the
@@ -136,18 +152,20 @@ k_batch_fixed(const InstDev* __restrict__ insts, const int* __restrict__ item_in
       sl[(b + 1) % 3].s = s;
       sl[(b + 1) % 3].kind = 1;
     }
-    const int tx = local % s_a.tiles_x;
-    const int rest = local / s_a.tiles_x;
-    const int ty = rest % s_a.tiles_y;
-    const int tz = rest / s_a.tiles_y;
+    // this thread's rectangle of the packed tile (lanes and warps past the
+    // last full rectangle join the last one, beyond its outputs)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncol = 32 / it.gw, nrow = W / it.gh;
+    const int col = min(lane / it.gw, ncol - 1);
+    const int rg = min(warp / it.gh, nrow - 1);
+    const fx::TileGroup grp = groups[it.group_base + rg * ncol + col];
     const int levels = min(K, steps - b * K);
     const int64_t* in = ((b & 1) ? arena1 : arena0) + I.offset;
     int64_t* out = ((b & 1) ? arena0 : arena1) + I.offset;
     unsigned long long my_or = 0ull;
-    const int z0 = tz * s_a.tz;
-    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs>(s_a, tx, ty, z0, min(s_a.tz, s_a.nz - z0),
-                                                     levels, b == 0, b == nblocks - 1, s, d, in,
-                                                     out, s_dyn, s_row, my_or);
+    fx::advance_tile<K, R, W, true, fx::kLoadL2Regs, false, false, true>(
+        s_a, 0, 0, 0, it.nout, levels, b == 0, b == nblocks - 1, s, d, in, out, s_dyn, s_row,
+        my_or, grp, lane - col * it.gw, (warp - rg * it.gh) * R);
     fx::cta_or<W>(my_or, s_or, &sl[(b + 1) % 3].m);
     __threadfence();
     __syncthreads();
@@ -264,18 +282,98 @@ void view3(const Geom& g, uint64_t n[3], double v[3], double L[3]) {
   }
 }
 
-// Stored order of an instance with view extents n: the permutation with the
-// fewest computed cells, tiles(n[p2]) * tiles(n[p1]) * n[p0] on tiles of 29
-// outputs per axis (depth 3); ties keep the view order.  Orders whose stored
-// plane has 2^31 cells or more are skipped (the fixed kernel's limit).
+// Packed tiles of one instance of nx x ny x nz cells (stored axes).  The x axis is cut
+// into segments of 32 - K outputs (a warp's width) and a remainder of rx
+// outputs (rx + K lanes); the y axis into ranges of R W - K outputs (all W
+// warps) and a remainder of ry outputs (ceil((ry + K) / R) warps).  The
+// rectangles of one size (lanes x warps) are packed side by side and stacked,
+// (32 / lanes) x (W / warps) to a tile.  To fill the tiles, the z axis of
+// those rectangles may be cut into s ranges of zl planes, each marched from
+// its own K warm-up planes; s minimises tiles x planes (with tz > 0, a range
+// holds at most tz planes).  The last range ends at the last plane and may
+// overlap the one before: the cells of the overlap are computed from the same
+// inputs by the same integer arithmetic in both and stored twice with the
+// same value, which no tile reads before the next time block.  Every other
+// output cell lies in exactly one rectangle.
+int pack_instance(int nx, int ny, int nz, int inst, int K, int R, int W, int tz,
+                  std::vector<ItemDev>* items, std::vector<fx::TileGroup>* groups) {
+  struct Seg {
+    int o, n, units;  // first output, outputs, lanes (x) or warps (y)
+  };
+  // [0]: full segments, [1]: the remainder (at most one)
+  std::vector<Seg> xs[2], ys[2];
+  const int Tx = 32 - K, Ty = R * W - K;
+  for (int j = 0; j < nx / Tx; ++j) xs[0].push_back({j * Tx, Tx, 32});
+  if (nx % Tx) xs[1].push_back({nx / Tx * Tx, nx % Tx, nx % Tx + K});
+  for (int j = 0; j < ny / Ty; ++j) ys[0].push_back({j * Ty, Ty, W});
+  if (ny % Ty) ys[1].push_back({ny / Ty * Ty, ny % Ty, (ny % Ty + K + R - 1) / R});
+  for (int xc = 0; xc < 2; ++xc) {
+    for (int yc = 0; yc < 2; ++yc) {
+      if (xs[xc].empty() || ys[yc].empty()) continue;
+      const int gw = xs[xc][0].units, gh = ys[yc][0].units;
+      const int ncol = 32 / gw, nrow = W / gh, P = ncol * nrow;
+      const int64_t c = (int64_t)xs[xc].size() * (int64_t)ys[yc].size();
+      // z ranges: the count sp of ranges that minimises tiles x planes
+      const int s_min = tz > 0 ? (nz + tz - 1) / tz : 1;
+      const int s_max = std::min(nz, std::max(s_min, P));
+      int zl_best = nz;
+      int64_t best_cost = INT64_MAX;
+      for (int sp = s_min; sp <= s_max; ++sp) {
+        const int64_t zl = (nz + sp - 1) / sp;
+        const int64_t zr = (nz + zl - 1) / zl;
+        const int64_t cost = ((c * zr + P - 1) / P) * (zl + K);
+        if (cost < best_cost) {
+          best_cost = cost;
+          zl_best = (int)zl;
+        }
+      }
+      const int zl = zl_best;
+      const int zr = (nz + zl - 1) / zl;
+      int in_item = 0;
+      for (const Seg& x : xs[xc]) {
+        for (const Seg& y : ys[yc]) {
+          for (int k = 0; k < zr; ++k) {
+            if (in_item == 0) items->push_back({inst, gw, gh, (int)groups->size(), zl});
+            fx::TileGroup g;
+            g.x0 = x.o;
+            g.xout = x.n;
+            g.y0 = y.o;
+            g.yout = y.n;
+            g.z0 = std::min(k * zl, nz - zl);
+            groups->push_back(g);
+            if (++in_item == P) in_item = 0;
+          }
+        }
+      }
+      // the last tile's unused rectangles store nothing
+      for (; in_item != 0 && in_item < P; ++in_item) groups->push_back(fx::TileGroup{});
+    }
+  }
+  return FDB_OK;
+}
+
+// Tiles x planes marched per time block by pack_instance's tiles.
+int64_t packed_cost(int nx, int ny, int nz, int K, int R, int W) {
+  std::vector<ItemDev> items;
+  std::vector<fx::TileGroup> groups;
+  pack_instance(nx, ny, nz, 0, K, R, W, 0, &items, &groups);
+  int64_t c = 0;
+  for (const ItemDev& it : items) c += it.nout + K;
+  return c;
+}
+
+// Stored order of an instance with view extents n: the permutation whose
+// packed tiles (pack_instance at the default depth 2 with 4 rows x 8 warps)
+// march the fewest tile-planes per time block; ties keep the view order.  Orders whose
+// stored plane has 2^31 cells or more are skipped (the fixed kernel's limit).
 std::array<int, 3> choose_order(const uint64_t n[3]) {
   static const int ps[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-  auto tiles = [](uint64_t m) { return (m + 28) / 29; };
   std::array<int, 3> best = {0, 1, 2};
-  uint64_t best_cost = UINT64_MAX;
+  int64_t best_cost = INT64_MAX;
   for (const auto& p : ps) {
-    if (n[p[1]] * n[p[2]] >= (1ull << 31)) continue;
-    const uint64_t cost = tiles(n[p[2]]) * tiles(n[p[1]]) * n[p[0]];
+    if (n[p[1]] * n[p[2]] >= (1ull << 31) || n[p[0]] >= (1ull << 31)) continue;
+    const int64_t cost =
+        packed_cost((int)n[p[2]], (int)n[p[1]], (int)n[p[0]], kDefaultDepth, 4, 8);
     if (cost < best_cost) {
       best_cost = cost;
       best = {p[0], p[1], p[2]};
@@ -285,7 +383,8 @@ std::array<int, 3> choose_order(const uint64_t n[3]) {
 }
 
 template <int K, int R, int W>
-int launch_batch_kernel(int grid, const InstDev* insts, const int* item_inst, int ipb,
+int launch_batch_kernel(int grid, const InstDev* insts, const ItemDev* items,
+                        const fx::TileGroup* groups, int ipb,
                         int nblocks, int steps, int64_t* a0, int64_t* a1, ScaleSlot* slots,
                         unsigned* done, unsigned* queue, int* err, unsigned wait_bias,
                         long long wait_cycles, cudaStream_t st) {
@@ -296,7 +395,7 @@ int launch_batch_kernel(int grid, const InstDev* insts, const int* item_inst, in
                          smem);
     configured = true;
   }
-  k_batch_fixed<K, R, W><<<grid, 32 * W, smem, st>>>(insts, item_inst, ipb, nblocks, steps, a0,
+  k_batch_fixed<K, R, W><<<grid, 32 * W, smem, st>>>(insts, items, groups, ipb, nblocks, steps, a0,
                                                      a1, slots, done, queue, err, wait_bias,
                                                      wait_cycles);
   return FDB_OK;
@@ -314,7 +413,8 @@ int resident_ctas_of() {
   return std::max(1, per_sm) * std::max(1, sms);
 }
 
-using LaunchFn = int (*)(int, const InstDev*, const int*, int, int, int, int64_t*, int64_t*,
+using LaunchFn = int (*)(int, const InstDev*, const ItemDev*, const fx::TileGroup*, int, int,
+                         int, int64_t*, int64_t*,
                          ScaleSlot*, unsigned*, unsigned*, int*, unsigned, long long,
                          cudaStream_t);
 using ResidentFn = int (*)();
@@ -381,8 +481,10 @@ struct fdb_batch {
   int cur = 0;
   // device tables
   InstDev* d_insts = nullptr;
-  int* d_item_inst = nullptr;
+  ItemDev* d_items = nullptr;
   size_t item_cap = 0;
+  fx::TileGroup* d_groups = nullptr;
+  size_t group_cap = 0;
   ScaleSlot* d_slots = nullptr;
   unsigned* d_done = nullptr;
   unsigned* d_queue = nullptr;
@@ -452,7 +554,8 @@ struct Plan {
   int K, shape, tz;
   const Variant* v;
   std::vector<InstDev> insts;
-  std::vector<int> item_inst;
+  std::vector<ItemDev> items;
+  std::vector<fx::TileGroup> groups;
   int ipb = 0;
   int nblocks = 0;
   int grid = 0;
@@ -465,8 +568,10 @@ int make_plan(fdb_batch* b, int steps, const double* dt, int K, int shape, int t
   p->v = find_variant(K, shape);
   if (!p->v) return fail(FDB_ERR_UNSUPPORTED, "no batched kernel compiled for this depth/shape");
   p->insts.resize(b->count);
-  p->item_inst.clear();
+  p->items.clear();
+  p->groups.clear();
   const int resident = p->v->resident();
+  const int R = fx::shape_rows(shape), W = fx::shape_warps(shape);
   int base = 0;
   for (int i = 0; i < b->count; ++i) {
     const Geom& g = b->geoms[i];
@@ -479,13 +584,16 @@ int make_plan(fdb_batch* b, int steps, const double* dt, int K, int shape, int t
                           tz > 0 ? tz : (int)g.nz, resident);
     I.a.scale_log = nullptr;
     I.offset = b->offsets[i];
-    const int64_t items = (int64_t)I.a.tiles_x * I.a.tiles_y * I.a.tiles_z;
-    if (items > (1 << 24)) return fail(FDB_ERR_UNSUPPORTED, "instance has too many tiles");
+    const size_t first = p->items.size();
+    FDB_TRY(pack_instance(I.a.nx, I.a.ny, I.a.nz, i, K, R, W, tz, &p->items, &p->groups));
+    const size_t items = p->items.size() - first;
+    if (items > (1u << 24)) return fail(FDB_ERR_UNSUPPORTED, "instance has too many tiles");
     I.items = (int)items;
     I.item_base = base;
-    for (int k = 0; k < I.items; ++k) p->item_inst.push_back(i);
     base += I.items;
   }
+  if (p->groups.size() >= (1ull << 31))
+    return fail(FDB_ERR_UNSUPPORTED, "batched plan exceeds 2^31 tile rectangles");
   p->ipb = base;
   p->nblocks = (steps + K - 1) / K;
   if ((int64_t)p->nblocks * p->ipb >= (1ll << 31))
@@ -507,7 +615,7 @@ int enqueue_advect(fdb_batch* b, const Plan& p, int steps, cudaStream_t st) {
   // FDB_FAULT=timeout makes every dependency unsatisfiable and the wait
   // budget ~1 ms, so the bounded-wait error path runs without a GPU fault
   const bool inject = fault_injected("timeout");
-  p.v->launch(p.grid, b->d_insts, b->d_item_inst, p.ipb, p.nblocks, steps, a0, a1, b->d_slots,
+  p.v->launch(p.grid, b->d_insts, b->d_items, b->d_groups, p.ipb, p.nblocks, steps, a0, a1, b->d_slots,
               b->d_done, b->d_queue, b->d_err, inject ? (1u << 30) : 0u,
               inject ? 2000000ll : kWaitCycles, st);
   note_launch(3);
@@ -516,16 +624,26 @@ int enqueue_advect(fdb_batch* b, const Plan& p, int steps, cudaStream_t st) {
 }
 
 int upload_plan(fdb_batch* b, const Plan& p) {
-  if (p.item_inst.size() > b->item_cap) {
-    if (b->d_item_inst) cudaFree(b->d_item_inst);
-    b->d_item_inst = nullptr;
-    FDB_TRY(balloc(&b->d_item_inst, p.item_inst.size()));
-    b->item_cap = p.item_inst.size();
+  if (p.items.size() > b->item_cap) {
+    if (b->d_items) cudaFree(b->d_items);
+    b->d_items = nullptr;
+    b->item_cap = 0;
+    FDB_TRY(balloc(&b->d_items, p.items.size()));
+    b->item_cap = p.items.size();
+  }
+  if (p.groups.size() > b->group_cap) {
+    if (b->d_groups) cudaFree(b->d_groups);
+    b->d_groups = nullptr;
+    b->group_cap = 0;
+    FDB_TRY(balloc(&b->d_groups, p.groups.size()));
+    b->group_cap = p.groups.size();
   }
   FDB_CUDA_TRY(cudaMemcpyAsync(b->d_insts, p.insts.data(), p.insts.size() * sizeof(InstDev),
                                cudaMemcpyHostToDevice, b->stream));
-  FDB_CUDA_TRY(cudaMemcpyAsync(b->d_item_inst, p.item_inst.data(),
-                               p.item_inst.size() * sizeof(int), cudaMemcpyHostToDevice,
+  FDB_CUDA_TRY(cudaMemcpyAsync(b->d_items, p.items.data(), p.items.size() * sizeof(ItemDev),
+                               cudaMemcpyHostToDevice, b->stream));
+  FDB_CUDA_TRY(cudaMemcpyAsync(b->d_groups, p.groups.data(),
+                               p.groups.size() * sizeof(fx::TileGroup), cudaMemcpyHostToDevice,
                                b->stream));
   return FDB_OK;
 }
@@ -628,7 +746,7 @@ int run_looped(fdb_batch* b, int steps, const double* dt, int K) {
   return FDB_OK;
 }
 
-int effective_K(fdb_batch* b) { return b->K > 0 ? b->K : 4; }
+int effective_K(fdb_batch* b) { return b->K > 0 ? b->K : kDefaultDepth; }
 
 void free_batch_adjoint(fdb_batch* b) {
   for (double* p : b->adj_ckpt) cudaFree(p);
@@ -768,7 +886,7 @@ int fdb_batch_destroy(fdb_batch* b) {
   if (!b) return FDB_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  void* ps[] = {b->arena[0], b->arena[1], b->d_insts, b->d_item_inst, b->d_slots, b->d_done,
+  void* ps[] = {b->arena[0], b->arena[1], b->d_insts, b->d_items, b->d_groups, b->d_slots, b->d_done,
                 b->d_queue, b->d_err, b->d_offs, b->d_sizes, b->d_part, b->d_sums,
                 b->d_plain_scratch, b->d_stage};
   for (void* p : ps)
@@ -1292,7 +1410,7 @@ int fdb_batch_autotune(fdb_batch* b, int num_steps, const double* dt, const char
     return fail(FDB_ERR_CUDA, "autotune: cudaEventCreate failed");
   }
   float best = 1e30f;
-  int bK = 4, bsh = fx::kR4W8S, btz = 0;
+  int bK = kDefaultDepth, bsh = fx::kR4W8S, btz = 0;
   int rc = FDB_OK;
   for (const Variant& v : kVariants) {
     for (int tzc : {0, 32}) {

@@ -123,6 +123,16 @@ __device__ __forceinline__ bool scale_from_slot(const ScaleSlot* slot, int guard
 // launch, like cp.async, but without the shared-memory staging).
 enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1, kLoadRegs = 2 };
 
+// One rectangle of a packed tile (the persistent batched kernel): the output
+// cells x in [x0, x0+xout), y in [y0, y0+yout) of the logical axes, and the
+// tile's planes from z0 on, computed by a block of lanes (xout + K of them at
+// most) and warps of the CTA.  xout = 0 marks an unused rectangle (nothing
+// stored).
+struct TileGroup {
+  int x0, y0, z0;
+  int xout, yout;
+};
+
 // Advance one tile of one field by `levels` (<= K) steps.  The tile's output
 // region is x in [X0, X0+tx), y in [Y0, Y0+ty), z in [Z0, Z0+nout) of the
 // logical axes (Z0 + nout <= nz); the CTA computes a (32) x (R*W) x (nout+K)
@@ -134,14 +144,23 @@ enum Loader { kLoadCpAsync = 0, kLoadL2Regs = 1, kLoadRegs = 2 };
 // before the update (the previous plane's were read just before), and lane l
 // reads lane l-1's slot after a warp barrier.  Same values, fewer FMA-pipe
 // moves than the 64-bit shuffle.
+//
+// GROUPED: the CTA holds several rectangles (TileGroup) side by side in lanes
+// and stacked in warps; this thread's rectangle is `grp`, in which it is lane
+// `xlane` and its row 0 is row `wrow0`.  The first K lanes and rows of every
+// rectangle are its halo: the x-1 and y-1 neighbours they read from another
+// rectangle feed only halo cells, whose values are never stored.  tile_x,
+// tile_y and Z0 are unused, and every rectangle marches nout + K planes.
 template <int K, int R, int W, bool HSM, int LOADER, bool STORE_G = false,
-          bool LEFT_SMEM = false>
+          bool LEFT_SMEM = false, bool GROUPED = false>
 __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int tile_y, int Z0,
                                              int nout, int levels, bool in_f64, bool out_f64, int s, int d,
                                              const int64_t* __restrict__ in,
                                              int64_t* __restrict__ out, int64_t* s_dyn,
                                              int64_t (*s_row)[W][32],
-                                             unsigned long long& my_or) {
+                                             unsigned long long& my_or,
+                                             const TileGroup& grp = TileGroup{}, int xlane = 0,
+                                             int wrow0 = 0) {
   constexpr int kThreads = 32 * W;
   int64_t(*s_pre)[R][kThreads] = reinterpret_cast<int64_t(*)[R][kThreads]>(s_dyn);
   int64_t(*s_hist)[R][kThreads] =
@@ -150,17 +169,18 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  const int X0 = tile_x * a.tx;
-  const int Y0 = tile_y * a.ty;
+  const int X0 = GROUPED ? grp.x0 : tile_x * a.tx;
+  const int Y0 = GROUPED ? grp.y0 : tile_y * a.ty;
+  const int xl = GROUPED ? xlane : lane;
 
-  const int lx = wrap_mod(X0 - K + lane, a.nx);
+  const int lx = wrap_mod(X0 - K + xl, a.nx);
   const int px = a.fx ? a.nx - 1 - lx : lx;
-  const bool out_x = (lane >= K) && (X0 + lane - K < a.nx);
+  const bool out_x = GROUPED ? (xl >= K && xl - K < grp.xout) : (lane >= K) && (X0 + lane - K < a.nx);
 
   // offset (py * nx + px) of each of this thread's rows, wrapped once here:
   // the rows stay the same for the whole z-march (unsigned: each address is
   // one 32 x 32 -> 64-bit multiply-add)
-  const int ly0 = Y0 - K + warp * R;
+  const int ly0 = Y0 - K + (GROUPED ? wrow0 : warp * R);
   unsigned roff[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -178,13 +198,15 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   unsigned row_mask = 0u;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int ry = warp * R + r;
-    if (out_x && ry >= K && Y0 + ry - K < a.ny) row_mask |= 1u << r;
+    const int ry = (GROUPED ? wrow0 : warp * R) + r;
+    if (out_x && ry >= K && (GROUPED ? ry - K < grp.yout : Y0 + ry - K < a.ny)) row_mask |= 1u << r;
   }
+
 
   int64_t hist[HSM ? 1 : K][R];
   int64_t cur[R];
   static_assert(!LEFT_SMEM || HSM, "the x-1 neighbour from shared memory needs the history there");
+  static_assert(!(GROUPED && STORE_G), "packed tiles store no adjoint states");
   int64_t pre[LOADER != kLoadCpAsync ? R : 1];
 #pragma unroll
   for (int t = 0; t < (HSM ? 1 : K); ++t)
@@ -198,7 +220,7 @@ __device__ __forceinline__ void advance_tile(const FixedArgs& a, int tile_x, int
   }
 
   // logical z of the plane being computed; advanced by one per iteration
-  int lz = wrap_mod(Z0 - K, a.nz);
+  int lz = wrap_mod((GROUPED ? grp.z0 : Z0) - K, a.nz);
   int64_t po = (int64_t)(a.fz ? a.nz - 1 - lz : lz) * plane_sz;
   {
     const int64_t* src = in + po;

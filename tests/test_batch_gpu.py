@@ -165,8 +165,9 @@ def test_permuted_storage_is_invisible(fdb, port):
     for s in specs:
         s["dt"] = 0.3 * min(Lj / nj / abs(vj) for Lj, nj, vj in zip(s["L"], s["n"], s["v"]))
     b = fdb.Batch([(s["v"], s["L"], s["n"]) for s in specs])
-    assert b.storage_order(0) == (1, 0, 2)
-    assert b.storage_order(1) == (0, 1, 2)
+    assert sorted(b.storage_order(0)) == [0, 1, 2]
+    assert b.storage_order(0) != (0, 1, 2)  # 200 planes of 40 x 33 tile worst as x or y
+    assert b.storage_order(1) == (0, 1, 2)  # ties keep the caller's order
     rng = np.random.default_rng(21)
     f0 = [rng.standard_normal(int(np.prod(s["n"]))) for s in specs]
     for k in range(len(specs)):
