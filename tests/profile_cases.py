@@ -9,7 +9,7 @@ profiling a single launch on a case of a few hundred MB
   advect N S  : N^3 sphere + noise field, v = (1, -0.7, 0.3), dt = 0.5/N,
                 three advect calls of S steps
   batch C S   : C seeded instances with axes in [32, 160] (the benchmark's
-                generator), three batched advects of S steps (depth 3,
+                generator), three batched advects of S steps (depth 2,
                 shape 4x8 with shared-memory history, whole-z tiles: the
                 tuning the autotuner picks for the benchmark's batch)
   filter N I  : 2-D N x N laplacian Filter (the reference laplacian
@@ -60,7 +60,7 @@ def batch_case(count: int, steps: int) -> float:
     b = Batch([(s["v"], s["L"], s["n"]) for s in specs])
     for k, s in enumerate(specs):
         b.init_sphere(k, s["center"], s["radius"], 0.0, 20261203 + k)
-    b.set_tuning(depth=3, shape=4, tile_z=0)
+    b.set_tuning(depth=2, shape=4, tile_z=0)
     dts = [s["dt"] for s in specs]
     for _ in range(3):
         b.advect(steps, dts)
