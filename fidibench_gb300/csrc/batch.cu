@@ -3,9 +3,12 @@
 // each instance is the reference's advect(), upwind/cxx/upwind.cxx:51-86).
 //
 // Work.  advect(steps) is cut into time blocks of K steps.  A work item is
-// one tile (as in step_fixed.cu) of one instance in one time block; items are
-// numbered block-major, instance, tile.  One persistent grid (the resident
-// CTAs of the device) takes items from an atomic counter in that order.
+// one packed tile of one instance in one time block: rectangles of output
+// cells laid side by side in the lanes and stacked in the warps of a CTA
+// (pack_instance), so that the remainder strips of uneven axes share CTAs
+// instead of padding one each.  Items are numbered block-major, instance,
+// tile.  One persistent grid (the resident CTAs of the device) takes items
+// from an atomic counter in that order.
 //
 // Dependencies.  A tile of block b reads its upstream halo from the
 // neighbouring tiles' block b-1 output, so before starting it waits until
@@ -17,11 +20,11 @@
 // bounded (clock64 budget): on expiry the CTA sets an error bit and leaves,
 // the others follow, and the host reports FDB_ERR_TIMEOUT.
 //
-// Storage order.  An instance's three axes may be stored permuted: the
-// marched axis (z, no tiling) is the one that wastes most on 29-cell tiles
-// and the other two are tiled.  The update sums exact integer products, so
-// the result does not depend on the order of the axes; set_field, get_field
-// and init_sphere translate between the caller's order and the stored one.
+// Storage order.  An instance's three axes may be stored permuted: the order
+// whose packed tiles march the fewest tile-planes (choose_order).  The update
+// sums exact integer products, so the result does not depend on the order of
+// the axes; set_field, get_field and init_sphere translate between the
+// caller's order and the stored one.
 // Instances that the single-field path advances in FP64 keep their order, so
 // the looped comparator stays bit-identical to fdb_upwind_advect for all.
 //
