@@ -22,15 +22,23 @@ import torch
 from .autograd import batch_advect_fn
 
 
-def instance_specs(count: int, n: int, seed: int, courant_sum: float = 0.5):
-    """Seeded velocities in [-1, 1]^3, dt = courant_sum * dx / sum_j |v_j|
-    (so sum_j a_j = courant_sum), sphere centres in [0.3, 0.7]^3 and radii in
-    [0.1, 0.25]."""
+def instance_specs(count: int, n: int, seed: int, courant_sum: float = 0.5,
+                   cfl_rule: str = "sum"):
+    """Seeded velocities in [-1, 1]^3, sphere centres in [0.3, 0.7]^3 and
+    radii in [0.1, 0.25].  dt: with cfl_rule "sum", courant_sum * dx /
+    sum_j |v_j| (so sum_j a_j = courant_sum, inside the scheme's stable
+    range); with "per_axis", courant_sum * min_j dx / |v_j| (each axis at that
+    Courant number, the sum up to three times it)."""
+    if cfl_rule not in ("sum", "per_axis"):
+        raise ValueError("cfl_rule is 'sum' or 'per_axis'")
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
         v = rng.uniform(-1.0, 1.0, size=3)
-        dt = courant_sum * (1.0 / n) / float(np.sum(np.abs(v)))
+        if cfl_rule == "sum":
+            dt = courant_sum * (1.0 / n) / float(np.sum(np.abs(v)))
+        else:
+            dt = courant_sum * (1.0 / n) / float(np.max(np.abs(v)))
         out.append({"v": tuple(float(x) for x in v), "dt": dt,
                     "center": tuple(float(x) for x in rng.uniform(0.3, 0.7, size=3)),
                     "radius": float(rng.uniform(0.1, 0.25))})
@@ -45,9 +53,9 @@ def sphere_field(n: int, center, radius: float, device) -> torch.Tensor:
 
 
 def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, seed: int = 1,
-            lr: float = 1.0, fd_check: bool = True, device=None) -> dict:
+            lr: float = 1.0, fd_check: bool = True, device=None, cfl_rule: str = "sum") -> dict:
     device = device or torch.device("cuda", torch.cuda.current_device())
-    specs = instance_specs(count, n, seed)
+    specs = instance_specs(count, n, seed, cfl_rule=cfl_rule)
     shapes = [(n, n, n)] * count
     vel = torch.tensor([sp["v"] for sp in specs], dtype=torch.float64)
     dts = [sp["dt"] for sp in specs]
@@ -94,7 +102,11 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
                      torch.linalg.norm(f_true.view(count, cells), dim=1)).cpu().numpy()
     el = time.perf_counter() - t0
     rel = misfit / misfit0
+    csum = [sp["dt"] * n * sum(abs(x) for x in sp["v"]) for sp in specs]
     return {"instances": count, "n": n, "time_steps": steps, "iterations": iters,
+            "cfl_rule": cfl_rule, "courant_sum_max": max(csum),
+            "unstable_instances": int(sum(c > 1.0 for c in csum)),
+            "data_max_abs": float(torch.max(torch.abs(data))),
             "seconds": el, "misfit_reduction_max": float(np.max(rel)), "misfit_reduction_median":
             float(np.median(rel)), "final_misfit_median": float(np.median(misfit)),
             "field_rel_err_median": float(np.median(field_err)),
@@ -105,4 +117,26 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
             "mode": "all instances per launch (batched advect, batched transposed advect)"}
 
 
-__all__ = ["recover", "instance_specs", "sphere_field"]
+def data_amplification(count: int = 64, n: int = 128, steps: int = 100, seed: int = 1,
+                       cfl_rule: str = "sum", device=None) -> dict:
+    """The data side of the recovery workload alone: advect the sphere fields
+    and report the Courant sums and how far the data grew (max |data| over the
+    instances, the sphere fields being in [0, 1])."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    specs = instance_specs(count, n, seed, cfl_rule=cfl_rule)
+    vel = torch.tensor([sp["v"] for sp in specs], dtype=torch.float64)
+    f_true = torch.cat([sphere_field(n, sp["center"], sp["radius"], device).view(-1)
+                        for sp in specs])
+    with torch.no_grad():
+        data = batch_advect_fn(f_true, vel, [(n, n, n)] * count, steps,
+                               [sp["dt"] for sp in specs])
+    per = torch.amax(torch.abs(data.view(count, -1)), dim=1).cpu().numpy()
+    csum = np.array([sp["dt"] * n * sum(abs(x) for x in sp["v"]) for sp in specs])
+    return {"cfl_rule": cfl_rule, "courant_sum_max": float(csum.max()),
+            "unstable_instances": int((csum > 1.0).sum()),
+            "data_max_abs": float(per.max()),
+            "data_max_abs_stable_instances": float(per[csum <= 1.0].max()) if (csum <= 1.0).any()
+            else None}
+
+
+__all__ = ["recover", "instance_specs", "sphere_field", "data_amplification"]
