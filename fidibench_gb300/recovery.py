@@ -60,6 +60,13 @@ def recover(count: int = 64, n: int = 128, steps: int = 100, iters: int = 20, se
     vel = torch.tensor([sp["v"] for sp in specs], dtype=torch.float64)
     dts = [sp["dt"] for sp in specs]
     cells = n ** 3
+    # torch loads its own elementwise and reduction kernels on first use
+    # (seconds on a fresh process): run them once on a tiny field first, so
+    # that the timed setup is this workload's own
+    with torch.no_grad():
+        w = sphere_field(4, (0.5, 0.5, 0.5), 0.25, device).view(1, -1)
+        float(torch.linalg.norm(w, dim=1).sum() + torch.max(torch.abs(w)) + (w ** 2).sum())
+    torch.cuda.synchronize(device)
     t0 = time.perf_counter()
     f_true = torch.cat([sphere_field(n, sp["center"], sp["radius"], device).view(-1)
                         for sp in specs])
