@@ -229,3 +229,24 @@ def test_packed_tiles_edge_shapes(fdb, port, depth, tile_z):
         assert rel_maxnorm(a.get_field(k), ref) <= FIELD_TOL, k
     a.close()
     c.close()
+
+
+@pytest.mark.parametrize("depth", [2, 3])
+def test_packed_tiles_larger_instances_bit_identical(fdb, depth):
+    """A few instances with axes above one tile width on every axis (full
+    tiles, remainders in x and y, z ranges split to fill the remainder
+    tiles), mixed with small ones: the persistent launch at the default
+    shape equals the single-field kernel looped at the same depth."""
+    from fidibench_gb300.batch import random_instances
+    specs = random_instances(4, 31, 90, 200) + random_instances(5, 37, 8, 40)
+    dts = [s["dt"] for s in specs]
+    a = make_batch(fdb, specs)
+    c = make_batch(fdb, specs)
+    a.set_tuning(depth=depth, shape=4, tile_z=0)
+    c.set_tuning(depth=depth)
+    a.advect(2 * depth + 1, dts)  # a last time block shorter than the depth
+    c.advect_looped(2 * depth + 1, dts)
+    for k in range(a.count):
+        assert np.array_equal(a.get_field(k), c.get_field(k)), k
+    a.close()
+    c.close()
