@@ -342,7 +342,7 @@ int pack_instance(int nx, int ny, int nz, int inst, int K, int R, int W, int tz,
             g.xout = x.n;
             g.y0 = y.o;
             g.yout = y.n;
-            g.z0 = std::min(k * zl, nz - zl);
+            g.z0 = (int)std::min<int64_t>((int64_t)k * zl, nz - zl);
             groups->push_back(g);
             if (++in_item == P) in_item = 0;
           }
@@ -366,9 +366,10 @@ int64_t packed_cost(int nx, int ny, int nz, int K, int R, int W) {
 }
 
 // Stored order of an instance with view extents n: the permutation whose
-// packed tiles (pack_instance at the default depth 2 with 4 rows x 8 warps)
-// march the fewest tile-planes per time block; ties keep the view order.  Orders whose
-// stored plane has 2^31 cells or more are skipped (the fixed kernel's limit).
+// packed tiles (pack_instance at the default depth with 4 rows x 8 warps)
+// march the fewest tile-planes per time block; ties keep the view order.
+// Orders whose stored plane has 2^31 cells or more are skipped (the fixed
+// kernel's limit).
 std::array<int, 3> choose_order(const uint64_t n[3]) {
   static const int ps[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
   std::array<int, 3> best = {0, 1, 2};
