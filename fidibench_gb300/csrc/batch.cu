@@ -93,9 +93,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 template <int K, int R, int W>
 __global__ void __launch_bounds__(32 * W, (R > 4 ? 512 : 1024) / (32 * W))
 k_batch_fixed(const InstDev* __restrict__ insts, const ItemDev* __restrict__ items,
-              const fx::TileGroup* __restrict__ groups, int items_per_block, int nblocks, int steps, int64_t* arena0, int64_t* arena1,
-              ScaleSlot* slots, unsigned* done, unsigned* queue, int* err, unsigned wait_bias,
-              long long wait_cycles) {
+              const fx::TileGroup* __restrict__ groups, int items_per_block, int nblocks,
+              int steps, int64_t* arena0, int64_t* arena1, ScaleSlot* slots, unsigned* done,
+              unsigned* queue, int* err, unsigned wait_bias, long long wait_cycles) {
   extern __shared__ __align__(16) int64_t s_dyn[];  // plane history [K][R][threads]
   __shared__ int64_t s_row[2][W][32];
   __shared__ unsigned long long s_or[W];
@@ -388,10 +388,9 @@ std::array<int, 3> choose_order(const uint64_t n[3]) {
 
 template <int K, int R, int W>
 int launch_batch_kernel(int grid, const InstDev* insts, const ItemDev* items,
-                        const fx::TileGroup* groups, int ipb,
-                        int nblocks, int steps, int64_t* a0, int64_t* a1, ScaleSlot* slots,
-                        unsigned* done, unsigned* queue, int* err, unsigned wait_bias,
-                        long long wait_cycles, cudaStream_t st) {
+                        const fx::TileGroup* groups, int ipb, int nblocks, int steps, int64_t* a0,
+                        int64_t* a1, ScaleSlot* slots, unsigned* done, unsigned* queue, int* err,
+                        unsigned wait_bias, long long wait_cycles, cudaStream_t st) {
   constexpr int smem = K * R * 32 * W * (int)sizeof(int64_t);
   static bool configured = false;
   if (!configured) {
@@ -399,8 +398,8 @@ int launch_batch_kernel(int grid, const InstDev* insts, const ItemDev* items,
                          smem);
     configured = true;
   }
-  k_batch_fixed<K, R, W><<<grid, 32 * W, smem, st>>>(insts, items, groups, ipb, nblocks, steps, a0,
-                                                     a1, slots, done, queue, err, wait_bias,
+  k_batch_fixed<K, R, W><<<grid, 32 * W, smem, st>>>(insts, items, groups, ipb, nblocks, steps,
+                                                     a0, a1, slots, done, queue, err, wait_bias,
                                                      wait_cycles);
   return FDB_OK;
 }
@@ -619,8 +618,8 @@ int enqueue_advect(fdb_batch* b, const Plan& p, int steps, cudaStream_t st) {
   // FDB_FAULT=timeout makes every dependency unsatisfiable and the wait
   // budget ~1 ms, so the bounded-wait error path runs without a GPU fault
   const bool inject = fault_injected("timeout");
-  p.v->launch(p.grid, b->d_insts, b->d_items, b->d_groups, p.ipb, p.nblocks, steps, a0, a1, b->d_slots,
-              b->d_done, b->d_queue, b->d_err, inject ? (1u << 30) : 0u,
+  p.v->launch(p.grid, b->d_insts, b->d_items, b->d_groups, p.ipb, p.nblocks, steps, a0, a1,
+              b->d_slots, b->d_done, b->d_queue, b->d_err, inject ? (1u << 30) : 0u,
               inject ? 2000000ll : kWaitCycles, st);
   note_launch(3);
   FDB_CUDA_TRY(cudaGetLastError());
@@ -890,9 +889,9 @@ int fdb_batch_destroy(fdb_batch* b) {
   if (!b) return FDB_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  void* ps[] = {b->arena[0], b->arena[1], b->d_insts, b->d_items, b->d_groups, b->d_slots, b->d_done,
-                b->d_queue, b->d_err, b->d_offs, b->d_sizes, b->d_part, b->d_sums,
-                b->d_plain_scratch, b->d_stage};
+  void* ps[] = {b->arena[0], b->arena[1], b->d_insts, b->d_items,  b->d_groups,
+                b->d_slots,  b->d_done,  b->d_queue, b->d_err,    b->d_offs,
+                b->d_sizes,  b->d_part,  b->d_sums,  b->d_plain_scratch, b->d_stage};
   for (void* p : ps)
     if (p) cudaFree(p);
   free_batch_adjoint(b);
